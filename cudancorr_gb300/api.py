@@ -1,0 +1,271 @@
+"""Python mirror of cudaNcorr's `ncorr` class over the engine's C ABI.
+
+The reference's public surface is a C++ class (include/cudaNcorr.hpp:10-68 of
+cudaNcorr); this module keeps its names and argument meaning:
+
+    corr = ncorr(box, 0, bins, isSurvey, ori)      # ncorr::ncorr (threeD)
+    corr.calculateD1D2D3(p1, p2, p3)               # N x 4 (x, y, z, w) arrays
+    corr.getTriBinsOut(); corr.getTriCountsOut(); corr.getPiBinsOut()
+
+Errors raise NcorrError, a RuntimeError, where the reference throws
+std::runtime_error. Arrays are numpy float64 (host) or CUDA tensors of
+float64 (device-resident inputs, torch only as a container). There is no CPU
+path: the shared library must be built (cudancorr_gb300.build) and a CUDA
+device present.
+"""
+from __future__ import annotations
+
+import ctypes
+import pathlib
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import build as _build
+
+NCORR_OK = 0
+NCORR_ERR_INVALID_ARGUMENT = 1
+NCORR_ERR_NOT_IMPLEMENTED = 2
+NCORR_ERR_CUDA = 3
+NCORR_ERR_OUT_OF_GRID = 4
+NCORR_ERR_CAPACITY = 5
+NCORR_ERR_NO_DEVICE = 6
+
+threeD, rppi, smu = 0, 1, 2  # ncorr::binType (include/cudaNcorr.hpp:12)
+
+# Every symbol the C header declares (include/ncorr_gb300.h).
+EXPORTS = (
+    "ncorr_create", "ncorr_create_rppi", "ncorr_destroy", "ncorr_calculate_d1d2d3",
+    "ncorr_calculate_d1d2d3_device", "ncorr_num_out", "ncorr_num_bins", "ncorr_get_tri_bins_out",
+    "ncorr_get_pi_bins_out", "ncorr_get_tri_counts_out", "ncorr_get_tri_counts_all",
+    "ncorr_get_stats", "ncorr_last_error", "survey_prep_cat", "survey_prep_cat2", "ncorr_logspace",
+)
+
+
+class NcorrError(RuntimeError):
+    """Raised where the reference throws std::runtime_error."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(message)
+        self.code = code
+
+
+class NcorrStats(ctypes.Structure):
+    _fields_ = [
+        ("ms_grid", ctypes.c_double), ("ms_count", ctypes.c_double), ("ms_fold", ctypes.c_double),
+        ("ms_total", ctypes.c_double), ("n_anchors", ctypes.c_uint64),
+        ("n_pair_evals", ctypes.c_uint64), ("n_pairs", ctypes.c_uint64),
+        ("n_exact_pairs", ctypes.c_uint64), ("n_exact_tris", ctypes.c_uint64),
+        ("triangles", ctypes.c_uint64), ("weighted", ctypes.c_int), ("symmetric", ctypes.c_int),
+        ("grid_ctas", ctypes.c_int), ("list_capacity", ctypes.c_int),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+_LIB: Optional[ctypes.CDLL] = None
+_D = ctypes.POINTER(ctypes.c_double)
+
+
+def library_path() -> pathlib.Path:
+    return _build.library_path()
+
+
+def load_library() -> ctypes.CDLL:
+    """Loads libcudancorr_gb300.so; raises if it has not been built."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = library_path()
+    if not path.exists():
+        raise NcorrError(NCORR_ERR_NO_DEVICE,
+                         f"{path} is missing: build it with `python -m cudancorr_gb300.build`")
+    lib = ctypes.CDLL(str(path))
+    i64, i32, vp = ctypes.c_int64, ctypes.c_int, ctypes.c_void_p
+    hp = ctypes.POINTER(vp)
+    sig = {
+        "ncorr_create": (i32, [_D, i32, _D, i32, i32, _D, hp]),
+        "ncorr_create_rppi": (i32, [_D, i32, _D, i32, i32, i32, _D, hp]),
+        "ncorr_destroy": (None, [vp]),
+        "ncorr_calculate_d1d2d3": (i32, [vp, _D, i64, _D, i64, _D, i64]),
+        "ncorr_calculate_d1d2d3_device": (i32, [vp, vp, i64, vp, i64, vp, i64, vp]),
+        "ncorr_num_out": (i64, [vp]),
+        "ncorr_num_bins": (i32, [vp]),
+        "ncorr_get_tri_bins_out": (i32, [vp, _D, i64]),
+        "ncorr_get_pi_bins_out": (i32, [vp, _D, i64, ctypes.POINTER(i64)]),
+        "ncorr_get_tri_counts_out": (i32, [vp, _D, i64]),
+        "ncorr_get_tri_counts_all": (i32, [vp, _D, i64]),
+        "ncorr_get_stats": (i32, [vp, ctypes.POINTER(NcorrStats)]),
+        "ncorr_last_error": (ctypes.c_char_p, []),
+        "survey_prep_cat": (i32, [_D, i64, _D, _D]),
+        "survey_prep_cat2": (i32, [_D, i64, _D, i64, _D, _D]),
+        "ncorr_logspace": (i32, [ctypes.c_double, ctypes.c_double, i32, _D]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def _check(rc: int) -> None:
+    if rc != NCORR_OK:
+        msg = load_library().ncorr_last_error().decode(errors="replace")
+        raise NcorrError(rc, msg)
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(_D)
+
+
+def _vec3(v: Sequence[float]) -> np.ndarray:
+    a = np.ascontiguousarray(np.asarray(v, dtype=np.float64).reshape(3))
+    return a
+
+
+def as_catalog(p) -> np.ndarray:
+    """N x 4 float64 C-contiguous view/copy of a catalogue (x, y, z, w)."""
+    a = np.asarray(p, dtype=np.float64)
+    if a.ndim != 2 or a.shape[1] != 4:
+        raise NcorrError(NCORR_ERR_INVALID_ARGUMENT, "catalogue must be an N x 4 array (x, y, z, w)")
+    return np.ascontiguousarray(a)
+
+
+class ncorr:
+    """threeD (r1, r2, r3) triangle counter, the reference's `ncorr` class."""
+
+    def __init__(self, box, bin_type, bins, isSurvey=False, ori=(0.0, 0.0, 0.0),
+                 numMinorBins: Optional[int] = None):
+        lib = load_library()
+        self._h = ctypes.c_void_p()
+        self._box = _vec3(box)
+        self._ori = _vec3(ori)
+        self._bins = np.ascontiguousarray(np.asarray(bins, dtype=np.float64))
+        if numMinorBins is not None:
+            rc = lib.ncorr_create_rppi(_dptr(self._box), int(bin_type), _dptr(self._bins),
+                                       len(self._bins), int(numMinorBins), int(bool(isSurvey)),
+                                       _dptr(self._ori), ctypes.byref(self._h))
+        else:
+            rc = lib.ncorr_create(_dptr(self._box), int(bin_type), _dptr(self._bins), len(self._bins),
+                                  int(bool(isSurvey)), _dptr(self._ori), ctypes.byref(self._h))
+        _check(rc)
+        self._lib = lib
+        self.isSurvey = bool(isSurvey)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            self._lib.ncorr_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def num_bins(self) -> int:
+        return int(self._lib.ncorr_num_bins(self._h))
+
+    def calculateD1D2D3(self, p1, p2, p3) -> None:
+        """Counts triangles with p1 as anchors (source/cudaNcorr.cu:220-430).
+
+        Host arrays go through the reference-facing C call (with its host to
+        device copies); CUDA tensors go through the device-resident entry.
+        Passing the same object for p2 and p3 (or all three) marks the
+        catalogues identical.
+        """
+        if _is_cuda_tensor(p1):
+            return self._calculate_device(p1, p2, p3)
+        arrays = {}
+        out = []
+        for p in (p1, p2, p3):
+            key = id(p)
+            if key not in arrays:
+                arrays[key] = as_catalog(p)
+            out.append(arrays[key])
+        a1, a2, a3 = out
+        _check(self._lib.ncorr_calculate_d1d2d3(self._h, _dptr(a1), a1.shape[0], _dptr(a2),
+                                                 a2.shape[0], _dptr(a3), a3.shape[0]))
+
+    def _calculate_device(self, p1, p2, p3, stream=None) -> None:
+        for t in (p1, p2, p3):
+            if not _is_cuda_tensor(t) or t.dim() != 2 or t.shape[1] != 4 or not t.is_contiguous():
+                raise NcorrError(NCORR_ERR_INVALID_ARGUMENT,
+                                 "device catalogues must be contiguous N x 4 float64 CUDA tensors")
+            if str(t.dtype) != "torch.float64":
+                raise NcorrError(NCORR_ERR_INVALID_ARGUMENT, "device catalogues must be float64")
+        s = ctypes.c_void_p(stream) if stream is not None else None
+        _check(self._lib.ncorr_calculate_d1d2d3_device(
+            self._h, ctypes.c_void_p(p1.data_ptr()), p1.shape[0], ctypes.c_void_p(p2.data_ptr()),
+            p2.shape[0], ctypes.c_void_p(p3.data_ptr()), p3.shape[0], s))
+
+    def getTriBinsOut(self) -> np.ndarray:
+        """(n_out, 3) bin mids (source/cudaNcorr.cu:106-108)."""
+        n = int(self._lib.ncorr_num_out(self._h))
+        out = np.zeros((n, 3), dtype=np.float64)
+        _check(self._lib.ncorr_get_tri_bins_out(self._h, _dptr(out), out.size))
+        return out
+
+    def getPiBinsOut(self) -> np.ndarray:
+        """Always empty for the threeD bin type (source/cudaNcorr.cu:110-112)."""
+        n = ctypes.c_int64(0)
+        buf = np.zeros(1, dtype=np.float64)
+        _check(self._lib.ncorr_get_pi_bins_out(self._h, _dptr(buf), 0, ctypes.byref(n)))
+        return np.zeros((n.value, 2), dtype=np.float64)
+
+    def getTriCountsOut(self) -> np.ndarray:
+        """Compacted counts of the last calculation (source/cudaNcorr.cu:114-116)."""
+        n = int(self._lib.ncorr_num_out(self._h))
+        out = np.zeros(n, dtype=np.float64)
+        _check(self._lib.ncorr_get_tri_counts_out(self._h, _dptr(out), n))
+        return out
+
+    def getTriCountsAll(self) -> np.ndarray:
+        """Full nb^3 histogram (the reference's private triCountsAll_)."""
+        nb = self.num_bins
+        out = np.zeros(nb ** 3, dtype=np.float64)
+        _check(self._lib.ncorr_get_tri_counts_all(self._h, _dptr(out), out.size))
+        return out
+
+    def stats(self) -> dict:
+        s = NcorrStats()
+        _check(self._lib.ncorr_get_stats(self._h, ctypes.byref(s)))
+        return s.as_dict()
+
+
+def _is_cuda_tensor(x) -> bool:
+    return hasattr(x, "is_cuda") and hasattr(x, "data_ptr") and bool(getattr(x, "is_cuda", False))
+
+
+def prep_cat_survey(cat1: np.ndarray, cat2: Optional[np.ndarray] = None):
+    """survey::prep_cat_survey (source/survey.cu:94-128): shifts the N x 4
+    float64 catalogue(s) in place into a positive box; returns (box, ori)."""
+    lib = load_library()
+    box = np.zeros(3)
+    ori = np.zeros(3)
+    for c in (cat1, cat2):
+        if c is not None and (c.dtype != np.float64 or not c.flags.c_contiguous or c.ndim != 2
+                              or c.shape[1] != 4):
+            raise NcorrError(NCORR_ERR_INVALID_ARGUMENT, "catalogues must be C-contiguous N x 4 float64")
+    if cat2 is None:
+        _check(lib.survey_prep_cat(_dptr(cat1), cat1.shape[0], _dptr(box), _dptr(ori)))
+    else:
+        _check(lib.survey_prep_cat2(_dptr(cat1), cat1.shape[0], _dptr(cat2), cat2.shape[0], _dptr(box),
+                                    _dptr(ori)))
+    return box, ori
+
+
+def logspace(start: float, end: float, n: int) -> np.ndarray:
+    """logspace (source/utils.cu:16-27)."""
+    out = np.zeros(n)
+    _check(load_library().ncorr_logspace(float(start), float(end), int(n), _dptr(out)))
+    return out

@@ -1,0 +1,657 @@
+// C ABI of the engine (include/ncorr_gb300.h): handle life cycle, host
+// orchestration of one calculateD1D2D3, result compaction.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <vector>
+
+#include "../../include/ncorr_gb300.h"
+#include "engine.cuh"
+#include "triangles.cuh"
+
+namespace ncorr_gb300 {
+void launch_assign(const double4_16a* in, int n, const Geom& g, int* cid, int* count, int* flags,
+                   unsigned* wmax_bits, cudaStream_t st);
+void launch_scan(const int* count, int ncell, int* start, int* cursor, cudaStream_t st);
+void launch_scatter(const double4_16a* in, int n, const Geom& g, const int* cid, int* cursor,
+                    double4_16a* pd, float4* pq, int* pc, cudaStream_t st);
+void launch_nbr_bound(const int* count, const Geom& g, int* out, cudaStream_t st);
+cudaError_t launch_triangles(const KArgs& a, bool survey, bool sym, bool weighted, int grid,
+                             size_t smem, cudaStream_t st);
+int triangles_occupancy(bool survey, bool sym, bool weighted, size_t smem);
+void launch_fold(const unsigned long long* counts, const unsigned long long* wsum, int nb,
+                 bool weighted, double factor, double inv_scale, double* out,
+                 unsigned long long* total, cudaStream_t st);
+}  // namespace ncorr_gb300
+
+using namespace ncorr_gb300;
+
+namespace {
+
+thread_local std::string t_err;
+
+int fail(int code, const std::string& msg) {
+  t_err = msg;
+  return code;
+}
+
+// Contraction pattern of the reference's sqrSep as compiled by nvcc for the
+// GB300 (established by running the reference kernel on adversarial inputs):
+// fma(dz, dz, fma(dy, dy, dx*dx)).
+constexpr int kDefaultFmaPattern = 1;
+
+// Budget of dynamic shared memory per CTA so that two CTAs share an SM.
+constexpr int kSmemBudget = 110 * 1024;
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= cap && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t b = std::max<size_t>(bytes, 256);
+    cudaError_t e = cudaMalloc(&p, b);
+    if (e == cudaSuccess) cap = b;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+  template <class T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+};
+
+struct CatDev {
+  DevBuf in, cid, count, start, cursor, pd, pq, pc;
+  int n = 0;
+};
+
+}  // namespace
+
+struct ncorr_handle {
+  int survey = 0;
+  double box[3] = {0, 0, 0};
+  double ori[3] = {0, 0, 0};
+  std::vector<double> edges, mids;
+  int nb = 0;
+  long ncell = 0;
+  Geom g;
+  std::vector<unsigned char> table;
+  std::vector<double> counts_all, counts_out, tri_bins_out;
+  ncorr_stats stats;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  CatDev cat[3];
+  DevBuf d_table, d_flags, d_wmax, d_work, d_bound, d_hist, d_out, d_stats, d_total;
+  DevBuf slab_e, slab_m, slab_p, slab_w;
+  bool table_uploaded = false;
+};
+
+namespace {
+
+float f32_down(double x) {
+  float f = static_cast<float>(x);
+  if (static_cast<double>(f) > x) f = std::nextafter(f, -std::numeric_limits<float>::infinity());
+  return f;
+}
+float f32_up(double x) {
+  float f = static_cast<float>(x);
+  if (static_cast<double>(f) < x) f = std::nextafter(f, std::numeric_limits<float>::infinity());
+  return f;
+}
+
+// FP32 error model. For an FP32 estimate v of the reference's double r^2 V
+// (either stage), |v - V| <= ka*v + kb with the constants below; the bound
+// follows from cell-local coordinates of magnitude <= r_max, offsets of
+// magnitude <= r_max, and three roundings in the sum of squares. Margins are
+// generous on purpose: a wider band only sends more candidates to the exact
+// path. The Heron margin proves the reference's FP32 sqrtf triangle test
+// from the same estimates.
+void set_error_model(Geom& g) {
+  const double u = std::ldexp(1.0, -24);
+  const double r2 = g.sqr_rmax;
+  g.ka = static_cast<float>(40.0 * u);
+  g.kb = static_cast<float>(28.0 * u * r2);
+  g.ha = static_cast<float>(128.0 * u);
+  g.hb = static_cast<float>(192.0 * u * r2);
+}
+
+// Bin table: entry i covers every v with rint(v * scale) == i. Its code is the
+// bin that contains the whole error band of every such v, kCodeReject when
+// the band lies outside (rmin^2, rmax^2), or kCodeCareful otherwise.
+void build_table(Geom& g, std::vector<unsigned char>& tab) {
+  const int n = kTableSize;
+  tab.assign(n, static_cast<unsigned char>(kCodeCareful));
+  const double vmax = g.sqr_rmax * 1.05;
+  const float scale = static_cast<float>((n - 2) / vmax);
+  g.tab_scale = scale;
+  g.tab_n = n;
+  const double ka = g.ka, kb = g.kb;
+  for (int i = 0; i < n; ++i) {
+    double lo = (i - 0.5) / static_cast<double>(scale);
+    double hi = (i + 0.5) / static_cast<double>(scale);
+    if (lo < 0) lo = 0;
+    if (i == n - 1) hi = std::numeric_limits<double>::infinity();
+    // Inflate slightly for the rounding of the band arithmetic itself.
+    const double blo = lo - (ka * lo + kb) * 1.01;
+    const double bhi = hi + (ka * hi + kb) * 1.01;
+    unsigned char code = static_cast<unsigned char>(kCodeCareful);
+    if (bhi <= g.sqr_rmin || blo >= g.sqr_rmax) {
+      code = static_cast<unsigned char>(kCodeReject);
+    } else if (blo > g.sqr_rmin && bhi < g.sqr_rmax) {
+      for (int b = 0; b < g.nb; ++b) {
+        if (g.sqr_bins[b] <= blo && bhi < g.sqr_bins[b + 1]) {
+          code = static_cast<unsigned char>(b);
+          break;
+        }
+      }
+    }
+    tab[i] = code;
+  }
+}
+
+#define CU(call)                                                              \
+  do {                                                                        \
+    cudaError_t e_ = (call);                                                  \
+    if (e_ != cudaSuccess)                                                    \
+      return fail(NCORR_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+int validate_catalog_ptr(const double* p, int64_t n) {
+  if (n < 0) return fail(NCORR_ERR_INVALID_ARGUMENT, "negative catalogue size");
+  if (n > 0 && !p) return fail(NCORR_ERR_INVALID_ARGUMENT, "null catalogue");
+  if (n > (int64_t(1) << 30)) return fail(NCORR_ERR_INVALID_ARGUMENT, "catalogue larger than 2^30 points");
+  return NCORR_OK;
+}
+
+// Builds the cell list of one catalogue already in device memory.
+int grid_catalog(ncorr_handle* h, int ci, const double4_16a* d_in, int n, cudaStream_t st) {
+  CatDev& c = h->cat[ci];
+  c.n = n;
+  const size_t nn = static_cast<size_t>(std::max(n, 1));
+  CU(c.cid.ensure(nn * sizeof(int)));
+  CU(c.count.ensure(h->ncell * sizeof(int)));
+  CU(c.start.ensure((h->ncell + 1) * sizeof(int)));
+  CU(c.cursor.ensure(h->ncell * sizeof(int)));
+  CU(c.pd.ensure(nn * sizeof(double4_16a)));
+  CU(c.pq.ensure(nn * sizeof(float4)));
+  CU(c.pc.ensure(nn * sizeof(int)));
+  CU(cudaMemsetAsync(c.count.p, 0, h->ncell * sizeof(int), st));
+  launch_assign(d_in, n, h->g, c.cid.as<int>(), c.count.as<int>(), h->d_flags.as<int>() + ci,
+                h->d_wmax.as<unsigned>(), st);
+  launch_scan(c.count.as<int>(), static_cast<int>(h->ncell), c.start.as<int>(), c.cursor.as<int>(), st);
+  launch_scatter(d_in, n, h->g, c.cid.as<int>(), c.cursor.as<int>(), c.pd.as<double4_16a>(),
+                 c.pq.as<float4>(), c.pc.as<int>(), st);
+  CU(cudaGetLastError());
+  return NCORR_OK;
+}
+
+Catalog view(const CatDev& c) {
+  Catalog v;
+  v.pd = c.pd.as<double4_16a>();
+  v.pq = c.pq.as<float4>();
+  v.pc = c.pc.as<int>();
+  v.start = c.start.as<int>();
+  v.count = c.count.as<int>();
+  v.n = c.n;
+  return v;
+}
+
+void compact(ncorr_handle* h) {
+  const int nb = h->nb;
+  h->counts_out.clear();
+  for (int i = 0; i < nb; ++i)
+    for (int j = i; j < nb; ++j)
+      for (int k = j; k < nb; ++k)
+        if (h->mids[k] <= h->mids[i] + h->mids[j])
+          h->counts_out.push_back(h->counts_all[k + j * nb + i * nb * nb]);
+}
+
+int run(ncorr_handle* h, const double4_16a* d1, int n1, const double4_16a* d2, int n2, const double4_16a* d3,
+        int n3, cudaStream_t st, const void* key1, const void* key2, const void* key3) {
+  auto t0 = std::chrono::steady_clock::now();
+  // Distinct catalogues: identical inputs are gridded once.
+  int role[3];
+  role[0] = 0;
+  role[1] = (key2 == key1 && n2 == n1) ? 0 : 1;
+  if (key3 == key2 && n3 == n2)
+    role[2] = role[1];
+  else if (key3 == key1 && n3 == n1)
+    role[2] = 0;
+  else
+    role[2] = 2;
+  const bool sym = role[1] == role[2];
+  const double4_16a* src[3] = {d1, d2, d3};
+  const int ns[3] = {n1, n2, n3};
+
+  CU(h->d_flags.ensure(8 * sizeof(int)));
+  CU(h->d_wmax.ensure(sizeof(unsigned)));
+  CU(h->d_work.ensure(sizeof(int)));
+  CU(h->d_bound.ensure(2 * sizeof(int)));
+  CU(h->d_stats.ensure(8 * sizeof(unsigned long long)));
+  CU(h->d_total.ensure(sizeof(unsigned long long)));
+  CU(cudaMemsetAsync(h->d_flags.p, 0, 8 * sizeof(int), st));
+  CU(cudaMemsetAsync(h->d_wmax.p, 0, sizeof(unsigned), st));
+  CU(cudaMemsetAsync(h->d_bound.p, 0, 2 * sizeof(int), st));
+  CU(cudaMemsetAsync(h->d_stats.p, 0, 8 * sizeof(unsigned long long), st));
+  CU(cudaMemsetAsync(h->d_total.p, 0, sizeof(unsigned long long), st));
+  if (!h->table_uploaded) {
+    CU(h->d_table.ensure(h->table.size()));
+    CU(cudaMemcpyAsync(h->d_table.p, h->table.data(), h->table.size(), cudaMemcpyHostToDevice, st));
+    h->table_uploaded = true;
+  }
+
+  CU(cudaEventRecord(h->ev[0], st));
+  bool done[3] = {false, false, false};
+  for (int r = 0; r < 3; ++r) {
+    int ci = role[r];
+    if (done[ci]) continue;
+    done[ci] = true;
+    int rc = grid_catalog(h, ci, src[r], ns[r], st);
+    if (rc) return rc;
+  }
+  launch_nbr_bound(h->cat[role[1]].count.as<int>(), h->g, h->d_bound.as<int>(), st);
+  if (!sym) launch_nbr_bound(h->cat[role[2]].count.as<int>(), h->g, h->d_bound.as<int>() + 1, st);
+  CU(cudaGetLastError());
+  CU(cudaEventRecord(h->ev[1], st));
+
+  int flags[8];
+  unsigned wmax_bits = 0;
+  int bound[2] = {0, 0};
+  CU(cudaMemcpyAsync(flags, h->d_flags.p, sizeof(flags), cudaMemcpyDeviceToHost, st));
+  CU(cudaMemcpyAsync(&wmax_bits, h->d_wmax.p, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+  CU(cudaMemcpyAsync(bound, h->d_bound.p, sizeof(bound), cudaMemcpyDeviceToHost, st));
+  CU(cudaStreamSynchronize(st));
+  bool weighted = false;
+  for (int r = 0; r < 3; ++r) {
+    const int f = flags[role[r]];
+    if (f & kFlagNonFinite) return fail(NCORR_ERR_OUT_OF_GRID, "non-finite coordinate or weight");
+    if (f & kFlagOutOfGrid)
+      return fail(NCORR_ERR_OUT_OF_GRID,
+                  "a point lies outside the cell grid of the box (the reference would index out of bounds)");
+    if (f & kFlagWeighted) weighted = true;
+  }
+  if (h->survey && (flags[role[0]] & kFlagSurveyFace))
+    return fail(NCORR_ERR_OUT_OF_GRID,
+                "survey anchor on the upper face of the cell grid (unclamped cell index == nc)");
+
+  // Fixed-point scale for weighted sums: |w1*w2*w3| * scale <= 2^30.
+  float wscale = 1.0f;
+  if (weighted) {
+    float wmax = 0.0f;
+    std::memcpy(&wmax, &wmax_bits, sizeof(float));
+    double p3 = static_cast<double>(wmax) * wmax * wmax;
+    int e = 0;
+    if (p3 > 0) e = static_cast<int>(std::floor(std::log2(std::ldexp(1.0, 30) / p3)));
+    e = std::max(-120, std::min(120, e));
+    wscale = static_cast<float>(std::ldexp(1.0, e));
+  }
+
+  // Shared-memory list capacity and overflow slabs.
+  const int nbin = h->nb * h->nb * h->nb;
+  int ks = 0;
+  {
+    SmemLayout L0 = make_layout(h->nb, 0, sym, weighted);
+    int per = (sym ? 1 : 2) * (16 + 4 + 4 + (weighted ? 4 : 0));
+    ks = (kSmemBudget - L0.total) / per;
+    ks = (ks / kTile) * kTile;
+    if (ks < kTile) ks = kTile;
+  }
+  SmemLayout L = make_layout(h->nb, ks, sym, weighted);
+  const size_t smem = static_cast<size_t>(L.total);
+  int occ = triangles_occupancy(h->survey != 0, sym, weighted, smem);
+  if (occ <= 0) return fail(NCORR_ERR_CUDA, "triangle kernel does not fit on the device");
+  int nsm = 0;
+  CU(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->device));
+  int grid = std::max(1, std::min(n1, nsm * occ));
+  const int kmax = std::max(bound[0], bound[1]);
+  int kg = std::max(0, kmax - ks);
+  kg = ((kg + kTile - 1) / kTile) * kTile;
+  const size_t slab_n = static_cast<size_t>(grid) * 2 * std::max(kg, 1);
+  CU(h->slab_e.ensure(slab_n * sizeof(float4)));
+  CU(h->slab_m.ensure(slab_n * sizeof(unsigned)));
+  CU(h->slab_p.ensure(slab_n * sizeof(int)));
+  if (weighted) CU(h->slab_w.ensure(slab_n * sizeof(float)));
+
+  const size_t hist_words = weighted ? 2 * static_cast<size_t>(nbin) : static_cast<size_t>(nbin);
+  CU(h->d_hist.ensure(hist_words * sizeof(unsigned long long)));
+  CU(cudaMemsetAsync(h->d_hist.p, 0, hist_words * sizeof(unsigned long long), st));
+  CU(cudaMemsetAsync(h->d_work.p, 0, sizeof(int), st));
+  CU(h->d_out.ensure(nbin * sizeof(double)));
+
+  KArgs a;
+  a.g = h->g;
+  a.c1 = view(h->cat[role[0]]);
+  a.c2 = view(h->cat[role[1]]);
+  a.c3 = view(h->cat[role[2]]);
+  a.table = h->d_table.as<unsigned char>();
+  a.work = h->d_work.as<int>();
+  a.flags = h->d_flags.as<int>() + 4;
+  a.hist.counts = weighted ? nullptr : h->d_hist.as<unsigned long long>();
+  a.hist.wsum = weighted ? h->d_hist.as<unsigned long long>() : nullptr;
+  a.slab_e = h->slab_e.as<float4>();
+  a.slab_m = h->slab_m.as<unsigned>();
+  a.slab_p = h->slab_p.as<int>();
+  a.slab_w = weighted ? h->slab_w.as<float>() : nullptr;
+  a.ks = ks;
+  a.kg = kg;
+  a.wscale = wscale;
+  a.stats = h->d_stats.as<unsigned long long>();
+
+  CU(cudaEventRecord(h->ev[2], st));
+  if (n1 > 0) CU(launch_triangles(a, h->survey != 0, sym, weighted, grid, smem, st));
+  CU(cudaEventRecord(h->ev[3], st));
+  launch_fold(a.hist.counts, a.hist.wsum, h->nb, weighted, sym ? 2.0 : 1.0, 1.0 / wscale,
+              h->d_out.as<double>(), h->d_total.as<unsigned long long>(), st);
+  CU(cudaGetLastError());
+  h->counts_all.assign(nbin, 0.0);
+  unsigned long long st_host[8];
+  unsigned long long total = 0;
+  int kflags = 0;
+  CU(cudaMemcpyAsync(h->counts_all.data(), h->d_out.p, nbin * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CU(cudaMemcpyAsync(st_host, h->d_stats.p, sizeof(st_host), cudaMemcpyDeviceToHost, st));
+  CU(cudaMemcpyAsync(&total, h->d_total.p, sizeof(total), cudaMemcpyDeviceToHost, st));
+  CU(cudaMemcpyAsync(&kflags, h->d_flags.as<int>() + 4, sizeof(int), cudaMemcpyDeviceToHost, st));
+  cudaEvent_t ev_end;
+  CU(cudaEventCreate(&ev_end));
+  CU(cudaEventRecord(ev_end, st));
+  CU(cudaStreamSynchronize(st));
+  if (kflags & kFlagListOverflow) return fail(NCORR_ERR_CAPACITY, "neighbour list overflow");
+  float ms0 = 0, ms1 = 0, ms2 = 0;
+  cudaEventElapsedTime(&ms0, h->ev[0], h->ev[1]);
+  cudaEventElapsedTime(&ms1, h->ev[2], h->ev[3]);
+  cudaEventElapsedTime(&ms2, h->ev[3], ev_end);
+  cudaEventDestroy(ev_end);
+  compact(h);
+  auto t1 = std::chrono::steady_clock::now();
+  ncorr_stats& s = h->stats;
+  s.ms_grid = ms0;
+  s.ms_count = ms1;
+  s.ms_fold = ms2;
+  s.ms_total = std::chrono::duration<double, std::milli>(t1 - t0).count();
+  s.n_exact_tris = st_host[0];
+  s.n_exact_pairs = st_host[1];
+  s.n_anchors = st_host[2];
+  s.n_pairs = st_host[3];
+  s.n_pair_evals = st_host[4];
+  s.triangles = weighted ? 0 : total;
+  s.weighted = weighted ? 1 : 0;
+  s.symmetric = sym ? 1 : 0;
+  s.grid_ctas = grid;
+  s.list_capacity = ks;
+  return NCORR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* ncorr_last_error(void) { return t_err.c_str(); }
+
+int ncorr_create(const double box[3], int bin_type, const double* edges, int n_edges, int is_survey,
+                 const double ori[3], ncorr_handle** out) {
+  if (!out) return fail(NCORR_ERR_INVALID_ARGUMENT, "null handle pointer");
+  *out = nullptr;
+  if (bin_type != NCORR_BIN_THREED)
+    return fail(NCORR_ERR_INVALID_ARGUMENT, "Invalid constructor call for bin_type.");
+  if (!box || !edges) return fail(NCORR_ERR_INVALID_ARGUMENT, "null box or edges");
+  if (n_edges < 2 || n_edges > kMaxEdges)
+    return fail(NCORR_ERR_INVALID_ARGUMENT, "need 2..128 bin edges");
+  for (int i = 0; i < n_edges; ++i)
+    if (!std::isfinite(edges[i])) return fail(NCORR_ERR_INVALID_ARGUMENT, "non-finite bin edge");
+  if (edges[0] < 0.0) return fail(NCORR_ERR_INVALID_ARGUMENT, "negative first bin edge");
+  for (int i = 1; i < n_edges; ++i)
+    if (!(edges[i] > edges[i - 1]) || !(edges[i] * edges[i] > edges[i - 1] * edges[i - 1]))
+      return fail(NCORR_ERR_INVALID_ARGUMENT, "bin edges must be strictly increasing");
+  for (int d = 0; d < 3; ++d)
+    if (!(box[d] > 0.0) || !std::isfinite(box[d]))
+      return fail(NCORR_ERR_INVALID_ARGUMENT, "box sides must be positive");
+  int dev_count = 0;
+  if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count <= 0)
+    return fail(NCORR_ERR_NO_DEVICE, "no CUDA device");
+
+  ncorr_handle* h = new ncorr_handle();
+  h->survey = is_survey ? 1 : 0;
+  for (int d = 0; d < 3; ++d) {
+    h->box[d] = box[d];
+    h->ori[d] = ori ? ori[d] : 0.0;
+  }
+  h->edges.assign(edges, edges + n_edges);
+  h->nb = n_edges - 1;
+  for (int i = 1; i < n_edges; ++i) h->mids.push_back((edges[i] + edges[i - 1]) / 2.0);
+  Geom& g = h->g;
+  std::memset(&g, 0, sizeof(g));
+  g.nb = h->nb;
+  g.survey = h->survey;
+  g.fma_pattern = kDefaultFmaPattern;
+  const double rmax = edges[n_edges - 1], rmin = edges[0];
+  g.cell = rmax;
+  g.sqr_rmax = rmax * rmax;
+  g.sqr_rmin = rmin * rmin;
+  long ncell = 1;
+  for (int d = 0; d < 3; ++d) {
+    g.box[d] = box[d];
+    double n = std::ceil(box[d] / rmax);
+    if (n > 4096.0) {
+      delete h;
+      return fail(NCORR_ERR_INVALID_ARGUMENT, "cell grid too large (box/r_max > 4096)");
+    }
+    g.nc[d] = static_cast<int>(n);
+    ncell *= g.nc[d];
+  }
+  if (ncell > (1L << 26)) {
+    delete h;
+    return fail(NCORR_ERR_INVALID_ARGUMENT, "cell grid too large (more than 2^26 cells)");
+  }
+  h->ncell = ncell;
+  for (int i = 0; i < n_edges; ++i) {
+    g.sqr_bins[i] = edges[i] * edges[i];
+    g.e2lo[i] = f32_down(g.sqr_bins[i]);
+    g.e2hi[i] = f32_up(g.sqr_bins[i]);
+  }
+  set_error_model(g);
+  build_table(g, h->table);
+  // Bin mids and the compacted (r1,r2,r3) table (source/cudaNcorr.cu:145-154).
+  for (int i = 0; i < h->nb; ++i)
+    for (int j = i; j < h->nb; ++j)
+      for (int k = j; k < h->nb; ++k)
+        if (h->mids[k] <= h->mids[i] + h->mids[j]) {
+          h->tri_bins_out.push_back(h->mids[i]);
+          h->tri_bins_out.push_back(h->mids[j]);
+          h->tri_bins_out.push_back(h->mids[k]);
+          h->counts_out.push_back(0.0);
+        }
+  h->counts_all.assign(static_cast<size_t>(h->nb) * h->nb * h->nb, 0.0);
+  std::memset(&h->stats, 0, sizeof(h->stats));
+  cudaGetDevice(&h->device);
+  cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+  for (int i = 0; i < 4 && e == cudaSuccess; ++i) e = cudaEventCreate(&h->ev[i]);
+  if (e != cudaSuccess) {
+    ncorr_destroy(h);
+    return fail(NCORR_ERR_CUDA, std::string("stream/event creation: ") + cudaGetErrorString(e));
+  }
+  *out = h;
+  return NCORR_OK;
+}
+
+int ncorr_create_rppi(const double box[3], int bin_type, const double* edges, int n_edges,
+                      int num_minor_bins, int is_survey, const double ori[3], ncorr_handle** out) {
+  (void)box;
+  (void)edges;
+  (void)n_edges;
+  (void)num_minor_bins;
+  (void)is_survey;
+  (void)ori;
+  if (out) *out = nullptr;
+  if (bin_type != NCORR_BIN_RPPI)
+    return fail(NCORR_ERR_INVALID_ARGUMENT, "Invalid constructor call for bin_type.");
+  return fail(NCORR_ERR_NOT_IMPLEMENTED, "the rppi bin type is not implemented by this engine");
+}
+
+void ncorr_destroy(ncorr_handle* h) {
+  if (!h) return;
+  for (auto& c : h->cat) {
+    c.in.release();
+    c.cid.release();
+    c.count.release();
+    c.start.release();
+    c.cursor.release();
+    c.pd.release();
+    c.pq.release();
+    c.pc.release();
+  }
+  for (DevBuf* b : {&h->d_table, &h->d_flags, &h->d_wmax, &h->d_work, &h->d_bound, &h->d_hist,
+                    &h->d_out, &h->d_stats, &h->d_total, &h->slab_e, &h->slab_m, &h->slab_p,
+                    &h->slab_w})
+    b->release();
+  for (auto& e : h->ev)
+    if (e) cudaEventDestroy(e);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}
+
+int ncorr_calculate_d1d2d3(ncorr_handle* h, const double* p1, int64_t n1, const double* p2,
+                           int64_t n2, const double* p3, int64_t n3) {
+  if (!h) return fail(NCORR_ERR_INVALID_ARGUMENT, "null handle");
+  int rc;
+  if ((rc = validate_catalog_ptr(p1, n1)) || (rc = validate_catalog_ptr(p2, n2)) ||
+      (rc = validate_catalog_ptr(p3, n3)))
+    return rc;
+  cudaStream_t st = h->stream;
+  const double* src[3] = {p1, p2, p3};
+  const int64_t ns[3] = {n1, n2, n3};
+  const double4_16a* dev[3] = {nullptr, nullptr, nullptr};
+  // Host -> device, each distinct array once.
+  for (int r = 0; r < 3; ++r) {
+    int same = -1;
+    for (int q = 0; q < r; ++q)
+      if (src[q] == src[r] && ns[q] == ns[r]) same = q;
+    if (same >= 0) {
+      dev[r] = dev[same];
+      continue;
+    }
+    DevBuf& b = h->cat[r].in;
+    CU(b.ensure(std::max<int64_t>(ns[r], 1) * sizeof(double4_16a)));
+    if (ns[r] > 0)
+      CU(cudaMemcpyAsync(b.p, src[r], ns[r] * sizeof(double4_16a), cudaMemcpyHostToDevice, st));
+    dev[r] = b.as<double4_16a>();
+  }
+  return run(h, dev[0], static_cast<int>(n1), dev[1], static_cast<int>(n2), dev[2],
+             static_cast<int>(n3), st, p1, p2, p3);
+}
+
+int ncorr_calculate_d1d2d3_device(ncorr_handle* h, const double* d_p1, int64_t n1,
+                                  const double* d_p2, int64_t n2, const double* d_p3, int64_t n3,
+                                  void* stream) {
+  if (!h) return fail(NCORR_ERR_INVALID_ARGUMENT, "null handle");
+  int rc;
+  if ((rc = validate_catalog_ptr(d_p1, n1)) || (rc = validate_catalog_ptr(d_p2, n2)) ||
+      (rc = validate_catalog_ptr(d_p3, n3)))
+    return rc;
+  for (const double* p : {d_p1, d_p2, d_p3})
+    if (p && (reinterpret_cast<uintptr_t>(p) & 15u))
+      return fail(NCORR_ERR_INVALID_ARGUMENT, "device catalogues must be 16-byte aligned");
+  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : h->stream;
+  return run(h, reinterpret_cast<const double4_16a*>(d_p1), static_cast<int>(n1),
+             reinterpret_cast<const double4_16a*>(d_p2), static_cast<int>(n2),
+             reinterpret_cast<const double4_16a*>(d_p3), static_cast<int>(n3), st, d_p1, d_p2, d_p3);
+}
+
+int64_t ncorr_num_out(const ncorr_handle* h) {
+  return h ? static_cast<int64_t>(h->counts_out.size()) : 0;
+}
+
+int ncorr_num_bins(const ncorr_handle* h) { return h ? h->nb : 0; }
+
+int ncorr_get_tri_bins_out(const ncorr_handle* h, double* out, int64_t cap) {
+  if (!h || !out) return fail(NCORR_ERR_INVALID_ARGUMENT, "null argument");
+  if (cap < static_cast<int64_t>(h->tri_bins_out.size()))
+    return fail(NCORR_ERR_INVALID_ARGUMENT, "output capacity too small");
+  std::memcpy(out, h->tri_bins_out.data(), h->tri_bins_out.size() * sizeof(double));
+  return NCORR_OK;
+}
+
+int ncorr_get_pi_bins_out(const ncorr_handle* h, double* out, int64_t cap, int64_t* n) {
+  (void)out;
+  (void)cap;
+  if (!h) return fail(NCORR_ERR_INVALID_ARGUMENT, "null handle");
+  if (n) *n = 0;
+  return NCORR_OK;
+}
+
+int ncorr_get_tri_counts_out(const ncorr_handle* h, double* out, int64_t cap) {
+  if (!h || !out) return fail(NCORR_ERR_INVALID_ARGUMENT, "null argument");
+  if (cap < static_cast<int64_t>(h->counts_out.size()))
+    return fail(NCORR_ERR_INVALID_ARGUMENT, "output capacity too small");
+  std::memcpy(out, h->counts_out.data(), h->counts_out.size() * sizeof(double));
+  return NCORR_OK;
+}
+
+int ncorr_get_tri_counts_all(const ncorr_handle* h, double* out, int64_t cap) {
+  if (!h || !out) return fail(NCORR_ERR_INVALID_ARGUMENT, "null argument");
+  if (cap < static_cast<int64_t>(h->counts_all.size()))
+    return fail(NCORR_ERR_INVALID_ARGUMENT, "output capacity too small");
+  std::memcpy(out, h->counts_all.data(), h->counts_all.size() * sizeof(double));
+  return NCORR_OK;
+}
+
+int ncorr_get_stats(const ncorr_handle* h, ncorr_stats* out) {
+  if (!h || !out) return fail(NCORR_ERR_INVALID_ARGUMENT, "null argument");
+  *out = h->stats;
+  return NCORR_OK;
+}
+
+static void minmax(const double* c, int64_t n, double mn[3], double mx[3]) {
+  for (int64_t i = 0; i < n; ++i)
+    for (int d = 0; d < 3; ++d) {
+      const double v = c[4 * i + d];
+      if (v < mn[d]) mn[d] = v;
+      if (v > mx[d]) mx[d] = v;
+    }
+}
+
+int survey_prep_cat2(double* c1, int64_t n1, double* c2, int64_t n2, double box[3], double ori[3]) {
+  if (!box || !ori || (n1 > 0 && !c1) || (n2 > 0 && !c2) || n1 < 0 || n2 < 0)
+    return fail(NCORR_ERR_INVALID_ARGUMENT, "null or negative argument");
+  double mn[3], mx[3];
+  for (int d = 0; d < 3; ++d) {
+    mn[d] = std::numeric_limits<double>::max();
+    mx[d] = std::numeric_limits<double>::lowest();
+  }
+  minmax(c1, n1, mn, mx);
+  if (c2) minmax(c2, n2, mn, mx);
+  for (int d = 0; d < 3; ++d) {
+    box[d] = mx[d] - mn[d] + 1.0;
+    ori[d] = -mn[d];
+  }
+  for (int64_t i = 0; i < n1; ++i)
+    for (int d = 0; d < 3; ++d) c1[4 * i + d] -= mn[d];
+  if (c2)
+    for (int64_t i = 0; i < n2; ++i)
+      for (int d = 0; d < 3; ++d) c2[4 * i + d] -= mn[d];
+  return NCORR_OK;
+}
+
+int survey_prep_cat(double* cat, int64_t n, double box[3], double ori[3]) {
+  return survey_prep_cat2(cat, n, nullptr, 0, box, ori);
+}
+
+int ncorr_logspace(double start, double end, int n, double* out) {
+  if (!out || n < 2) return fail(NCORR_ERR_INVALID_ARGUMENT, "need n >= 2 and an output array");
+  const double a = std::log10(start), b = std::log10(end);
+  const double step = (b - a) / (n - 1);
+  for (int i = 0; i < n; ++i) out[i] = std::pow(10, a + i * step);
+  return NCORR_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,127 @@
+// Internal definitions shared by the engine's CUDA translation units.
+//
+// Data layout in HBM (one "catalogue" = one std::vector<double4> argument of
+// the reference's calculateD1D2D3):
+//   pd[n]    double4  exact (x, y, z, w), grouped by cell          32 B/point
+//   pq[n]    float4   (x - o_c, y - o_c, z - o_c, w) in FP32, o_c = the
+//                     cell's lower corner (cell-local coordinates)    16 B/point
+//   pc[n]    int      flat cell id of each sorted point               4 B/point
+//   start/count[ncell] int   cell offsets of the cell list
+// The cell grid is the reference's: cell edge = r_max, nc = ceil(box/r_max),
+// flat id z + nc.z*(y + nc.y*x) (source/cudaNcorr.cu:50-58, :137-140).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace ncorr_gb300 {
+
+constexpr int kMaxEdges = 128;   // nb <= 127
+constexpr int kThreads = 256;    // triangle kernel CTA
+constexpr int kWarps = kThreads / 32;
+constexpr int kReg = 4;          // list entries per lane held in registers
+constexpr int kTile = 32 * kReg; // tile edge of the pair loop
+constexpr int kQueueCap = 256;   // per-warp queue of exact-path candidates
+constexpr int kTableSize = 8192; // bin table entries (u8)
+
+// Bin codes returned by the FP32 classifiers.
+constexpr unsigned kCodeReject = 0xFEu;
+constexpr unsigned kCodeCareful = 0xFFu;
+
+// Error flags written by kernels.
+constexpr int kFlagOutOfGrid = 1;     // a point the reference would index out of bounds
+constexpr int kFlagNonFinite = 2;
+constexpr int kFlagSurveyFace = 4;    // survey anchor whose unclamped cell index is nc
+constexpr int kFlagListOverflow = 8;  // neighbour list exceeded its slab (host bug)
+constexpr int kFlagWeighted = 16;     // some weight != 1.0 (informational)
+
+struct Geom {
+  int nb;                 // bins per side
+  int nc[3];              // cells per axis
+  int survey;             // 1: clipped neighbours, no image shift
+  int fma_pattern;        // contraction of the reference's sqrSep
+  double box[3];
+  double cell;            // = r_max
+  double sqr_rmin, sqr_rmax;
+  double sqr_bins[kMaxEdges];  // edges^2 as the reference computes them (double)
+  float e2lo[kMaxEdges];       // largest float <= edges^2
+  float e2hi[kMaxEdges];       // smallest float >= edges^2
+  // FP32 error model: |v - V| <= ka*v + kb for every FP32 r^2 estimate v of
+  // the reference's double r^2 V (pair and triangle stage alike).
+  float ka, kb;
+  // Heron margin: a candidate triangle is certainly accepted by the
+  // reference's FP32 sqrtf test when H > S*(ha*S + hb), S = a+b+c.
+  float ha, hb;
+  // Bin table: code of r^2 = table[rint(v*tab_scale)], clamped to the last entry.
+  float tab_scale;
+  int tab_n;
+};
+
+struct Catalog {
+  const double4_16a* pd;
+  const float4* pq;
+  const int* pc;
+  const int* start;
+  const int* count;
+  int n;
+};
+
+// Fixed-point weighted sums are kept as signed 128-bit integers in two u64
+// words per bin: lo at [2*b], hi at [2*b+1].
+struct HistOut {
+  unsigned long long* counts;  // nb^3 unsorted keys (count mode)
+  unsigned long long* wsum;    // 2*nb^3 (weighted mode)
+};
+
+// Sum of squares of the reference's sqrSep (source/device.cu:30-36) under
+// the contraction pattern the CUDA compiler applied to it; the explicit
+// intrinsics keep this code from being contracted differently.
+__device__ __forceinline__ double sqr_sum_exact(double dx, double dy, double dz, int pattern) {
+  switch (pattern) {
+    case 0:
+      return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+    case 1:
+      return __fma_rn(dz, dz, __fma_rn(dy, dy, __dmul_rn(dx, dx)));
+    case 2:
+      return __fma_rn(dz, dz, __fma_rn(dx, dx, __dmul_rn(dy, dy)));
+    case 3:
+      return __fma_rn(dz, dz, __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+    case 4:
+      return __dadd_rn(__fma_rn(dy, dy, __dmul_rn(dx, dx)), __dmul_rn(dz, dz));
+    default:
+      return __dadd_rn(__fma_rn(dx, dx, __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+  }
+}
+
+__device__ __forceinline__ double sqr_sep_exact(double ax, double ay, double az, double bx,
+                                                double by, double bz, int pattern) {
+  return sqr_sum_exact(__dsub_rn(ax, bx), __dsub_rn(ay, by), __dsub_rn(az, bz), pattern);
+}
+
+// Bin of an exact r^2 already known to lie in (rmin^2, rmax^2): the unique b
+// with sqr_bins[b] <= r < sqr_bins[b+1] (source/device.cu:181-191).
+__device__ __forceinline__ int exact_bin(double r, const double* sqr_bins, int nb) {
+  int lo = 0, hi = nb - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (r >= sqr_bins[mid])
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+// The reference's FP32 triangle test (source/device.cu:163-175) on three
+// exact r^2 values: true when the triangle is kept.
+__device__ __forceinline__ bool exact_triangle_ok(double r1, double r2, double r3) {
+  double t;
+  if (r1 > r2) { t = r1; r1 = r2; r2 = t; }
+  if (r1 > r3) { t = r1; r1 = r3; r3 = t; }
+  if (r2 > r3) { t = r2; r2 = r3; r3 = t; }
+  float s1 = __fsqrt_rn(__double2float_rn(r1));
+  float s2 = __fsqrt_rn(__double2float_rn(r2));
+  float s3 = __fsqrt_rn(__double2float_rn(r3));
+  return !(__fadd_rn(s1, s2) <= s3);
+}
+
+}  // namespace ncorr_gb300

@@ -1,0 +1,103 @@
+// Instantiations and launchers of the triangle kernel, plus the histogram fold.
+#include "triangles.cuh"
+
+namespace ncorr_gb300 {
+
+template <bool SV, bool SYM, bool W>
+static cudaError_t launch_one(const KArgs& a, int grid, size_t smem, cudaStream_t st) {
+  cudaError_t e = cudaFuncSetAttribute(k_triangles<SV, SYM, W>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(smem));
+  if (e != cudaSuccess) return e;
+  k_triangles<SV, SYM, W><<<grid, kThreads, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
+template <bool SV, bool SYM, bool W>
+static int occupancy_one(size_t smem) {
+  cudaFuncSetAttribute(k_triangles<SV, SYM, W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       static_cast<int>(smem));
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_triangles<SV, SYM, W>, kThreads, smem) !=
+      cudaSuccess)
+    return 0;
+  return n;
+}
+
+cudaError_t launch_triangles(const KArgs& a, bool survey, bool sym, bool weighted, int grid,
+                             size_t smem, cudaStream_t st) {
+  if (survey) {
+    if (sym) return weighted ? launch_one<true, true, true>(a, grid, smem, st)
+                             : launch_one<true, true, false>(a, grid, smem, st);
+    return weighted ? launch_one<true, false, true>(a, grid, smem, st)
+                    : launch_one<true, false, false>(a, grid, smem, st);
+  }
+  if (sym) return weighted ? launch_one<false, true, true>(a, grid, smem, st)
+                           : launch_one<false, true, false>(a, grid, smem, st);
+  return weighted ? launch_one<false, false, true>(a, grid, smem, st)
+                  : launch_one<false, false, false>(a, grid, smem, st);
+}
+
+int triangles_occupancy(bool survey, bool sym, bool weighted, size_t smem) {
+  if (survey) {
+    if (sym) return weighted ? occupancy_one<true, true, true>(smem) : occupancy_one<true, true, false>(smem);
+    return weighted ? occupancy_one<true, false, true>(smem) : occupancy_one<true, false, false>(smem);
+  }
+  if (sym) return weighted ? occupancy_one<false, true, true>(smem) : occupancy_one<false, true, false>(smem);
+  return weighted ? occupancy_one<false, false, true>(smem) : occupancy_one<false, false, false>(smem);
+}
+
+// Folds the unsorted (bin_j, bin_l, bin_3) histogram into the reference's
+// triCountsAll_ layout: out[hi + mid*nb + lo*nb^2] for lo <= mid <= hi sums
+// the distinct permutations in a fixed order (deterministic), times `factor`
+// (2 when only pairs j < l were visited).
+__global__ void k_fold(const unsigned long long* __restrict__ counts,
+                       const unsigned long long* __restrict__ wsum, int nb, int weighted,
+                       double factor, double inv_scale, double* __restrict__ out,
+                       unsigned long long* __restrict__ total) {
+  const int nbin = nb * nb * nb;
+  int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nbin) return;
+  int hi = f % nb, mid = (f / nb) % nb, lo = f / (nb * nb);
+  if (!(lo <= mid && mid <= hi)) {
+    out[f] = 0.0;
+    return;
+  }
+  const int v[3] = {lo, mid, hi};
+  const int perm[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+  int seen[6];
+  int ns = 0;
+  double acc = 0.0;
+  unsigned long long cnt = 0;
+  for (int p = 0; p < 6; ++p) {
+    int key = (v[perm[p][0]] * nb + v[perm[p][1]]) * nb + v[perm[p][2]];
+    bool dup = false;
+    for (int q = 0; q < ns; ++q) dup = dup || (seen[q] == key);
+    if (dup) continue;
+    seen[ns++] = key;
+    if (weighted) {
+      long long whi = static_cast<long long>(wsum[2 * key + 1]);
+      unsigned long long wlo = wsum[2 * key];
+      acc += (static_cast<double>(whi) * 18446744073709551616.0 + static_cast<double>(wlo)) * inv_scale;
+    } else {
+      cnt += counts[key];
+    }
+  }
+  if (weighted) {
+    out[f] = acc * factor;
+  } else {
+    unsigned long long c = cnt * static_cast<unsigned long long>(factor);
+    out[f] = static_cast<double>(c);
+    if (c) atomicAdd(total, c);
+  }
+}
+
+void launch_fold(const unsigned long long* counts, const unsigned long long* wsum, int nb,
+                 bool weighted, double factor, double inv_scale, double* out,
+                 unsigned long long* total, cudaStream_t st) {
+  int nbin = nb * nb * nb;
+  k_fold<<<(nbin + 255) / 256, 256, 0, st>>>(counts, wsum, nb, weighted ? 1 : 0, factor, inv_scale,
+                                             out, total);
+}
+
+}  // namespace ncorr_gb300
