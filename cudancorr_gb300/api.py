@@ -38,7 +38,8 @@ EXPORTS = (
     "ncorr_create", "ncorr_create_rppi", "ncorr_destroy", "ncorr_calculate_d1d2d3",
     "ncorr_calculate_d1d2d3_device", "ncorr_num_out", "ncorr_num_bins", "ncorr_get_tri_bins_out",
     "ncorr_get_pi_bins_out", "ncorr_get_tri_counts_out", "ncorr_get_tri_counts_all",
-    "ncorr_get_stats", "ncorr_last_error", "survey_prep_cat", "survey_prep_cat2", "ncorr_logspace",
+    "ncorr_get_stats", "ncorr_last_error", "survey_prep_cat", "survey_prep_cat2",
+    "survey_convert_coordinates", "ncorr_logspace",
 )
 
 
@@ -100,6 +101,7 @@ def load_library() -> ctypes.CDLL:
         "ncorr_last_error": (ctypes.c_char_p, []),
         "survey_prep_cat": (i32, [_D, i64, _D, _D]),
         "survey_prep_cat2": (i32, [_D, i64, _D, i64, _D, _D]),
+        "survey_convert_coordinates": (i32, [_D, _D, i64, _D]),
         "ncorr_logspace": (i32, [ctypes.c_double, ctypes.c_double, i32, _D]),
     }
     for name, (res, args) in sig.items():
@@ -262,6 +264,16 @@ def prep_cat_survey(cat1: np.ndarray, cat2: Optional[np.ndarray] = None):
         _check(lib.survey_prep_cat2(_dptr(cat1), cat1.shape[0], _dptr(cat2), cat2.shape[0], _dptr(box),
                                     _dptr(ori)))
     return box, ori
+
+
+def convert_coordinates(catalog: np.ndarray, H0: float, OmegaM: float, OmegaLambda: float) -> np.ndarray:
+    """survey::convert_coordinates (source/survey.cu:39-57): (RA, Dec, z, w)
+    rows to comoving (x, y, z, w) in Mpc/h."""
+    a = as_catalog(catalog)
+    out = np.empty_like(a)
+    c = np.array([H0, OmegaM, OmegaLambda], dtype=np.float64)
+    _check(load_library().survey_convert_coordinates(_dptr(c), _dptr(a), a.shape[0], _dptr(out)))
+    return out
 
 
 def logspace(start: float, end: float, n: int) -> np.ndarray:

@@ -39,9 +39,9 @@ int fail(int code, const std::string& msg) {
 }
 
 // Contraction pattern of the reference's sqrSep as compiled by nvcc for the
-// GB300 (established by running the reference kernel on adversarial inputs):
-// fma(dz, dz, fma(dy, dy, dx*dx)).
-constexpr int kDefaultFmaPattern = 1;
+// GB300, established by running the reference kernel on inputs built to
+// separate the candidates: fma(dz, dz, fma(dx, dx, dy*dy)).
+constexpr int kDefaultFmaPattern = 2;
 
 // Budget of dynamic shared memory per CTA so that two CTAs share an SM.
 constexpr int kSmemBudget = 110 * 1024;
@@ -110,20 +110,36 @@ float f32_up(double x) {
   return f;
 }
 
-// FP32 error model. For an FP32 estimate v of the reference's double r^2 V
-// (either stage), |v - V| <= ka*v + kb with the constants below; the bound
-// follows from cell-local coordinates of magnitude <= r_max, offsets of
-// magnitude <= r_max, and three roundings in the sum of squares. Margins are
-// generous on purpose: a wider band only sends more candidates to the exact
-// path. The Heron margin proves the reference's FP32 sqrtf triangle test
-// from the same estimates.
+// FP32 error model (u = 2^-24).
+//  * List entries hold d = fl32(D), D the exact anchor-relative offset
+//    (computed in FP64), |D| < r_max. The pair estimate a = fl32(|d|^2)
+//    satisfies |a - A| <= 5u A; the triangle estimate v = fl32(|d_j - d_l|^2)
+//    satisfies |v - V| <= 7u V + 2u r_max^2 (componentwise error
+//    u(|D_j| + |D_l| + |X|), Cauchy-Schwarz, AM-GM on the cross term, three
+//    roundings in the sum of squares). ka, kb bound both with margin, also
+//    covering the rounding of the band arithmetic itself.
+//  * The prefilter estimate from cell-local coordinates (error <= 5u*cell +
+//    u|D| per component) satisfies |v - V| <= 14u V + 9u r_max^2; only used
+//    to skip candidates that are certainly out of range (pa, pb).
+//  * Heron: with |x - X| <= ka x + kb for all three sides, the exact Heron
+//    product H = 4ab - (c-a-b)^2 moves by <= 2S(ka S + 3 kb), its FP32
+//    evaluation errs by <= 6u S^2, and H >= 8.3u c_max^2 proves that the
+//    reference's FP32 sqrtf test keeps the triangle. Hence the test
+//    H > S (ha S + hb).
+// Margins are generous on purpose: a wider band only sends more candidates
+// to the exact FP64 path.
 void set_error_model(Geom& g) {
   const double u = std::ldexp(1.0, -24);
   const double r2 = g.sqr_rmax;
-  g.ka = static_cast<float>(40.0 * u);
-  g.kb = static_cast<float>(28.0 * u * r2);
-  g.ha = static_cast<float>(128.0 * u);
-  g.hb = static_cast<float>(192.0 * u * r2);
+  g.ka = static_cast<float>(12.0 * u);
+  g.kb = static_cast<float>(4.0 * u * r2);
+  g.ha = static_cast<float>(48.0 * u);
+  g.hb = static_cast<float>(32.0 * u * r2);
+  // Prefilter thresholds: candidates with v >= pre_hi or v <= pre_lo are
+  // certainly outside (r_min^2, r_max^2).
+  const double eb = 20.0 * u, ec = 12.0 * u * r2;
+  g.pre_hi = f32_up((r2 + ec) / (1.0 - eb) * (1.0 + 4.0 * u));
+  g.pre_lo = f32_down((g.sqr_rmin - ec) / (1.0 + eb) * (1.0 - 4.0 * u) - 4.0 * u * ec);
 }
 
 // Bin table: entry i covers every v with rint(v * scale) == i. Its code is the
@@ -644,6 +660,70 @@ int survey_prep_cat2(double* c1, int64_t n1, double* c2, int64_t n2, double box[
 
 int survey_prep_cat(double* cat, int64_t n, double box[3], double ori[3]) {
   return survey_prep_cat2(cat, n, nullptr, 0, box, ori);
+}
+
+// Gauss-Legendre nodes and weights on [-1, 1] by Newton iteration on P_n.
+static void gauss_legendre(int n, std::vector<double>& x, std::vector<double>& w) {
+  x.assign(n, 0.0);
+  w.assign(n, 0.0);
+  const double pi = 3.14159265358979323846;
+  for (int i = 0; i < (n + 1) / 2; ++i) {
+    double z = std::cos(pi * (i + 0.75) / (n + 0.5)), dp = 0.0;
+    for (int it = 0; it < 100; ++it) {
+      double p0 = 1.0, p1 = 0.0;
+      for (int k = 1; k <= n; ++k) {
+        const double p2 = p1;
+        p1 = p0;
+        p0 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p2) / k;
+      }
+      dp = n * (z * p0 - p1) / (z * z - 1.0);
+      const double dz = p0 / dp;
+      z -= dz;
+      if (std::fabs(dz) < 1e-16) break;
+    }
+    x[i] = -z;
+    x[n - 1 - i] = z;
+    w[i] = w[n - 1 - i] = 2.0 / ((1.0 - z * z) * dp * dp);
+  }
+}
+
+int survey_convert_coordinates(const double cosmo[3], const double* in, int64_t n, double* out) {
+  if (!cosmo || n < 0 || (n > 0 && (!in || !out)))
+    return fail(NCORR_ERR_INVALID_ARGUMENT, "null or negative argument");
+  const double om = cosmo[1], ol = cosmo[2];
+  const double c_over_100 = 299792.458 / 100.0;  // source/survey.cu:12, :36
+  const double deg = 3.14159265358979323846 / 180.0;
+  static std::vector<double> gx, gw;
+  static bool init = false;
+  if (!init) {
+    gauss_legendre(48, gx, gw);
+    init = true;
+  }
+  // 1/E(z) is smooth on [0, z]; 48-point Gauss-Legendre on panels of width
+  // <= 0.5 in z converges to ~1e-15 relative.
+  auto dist = [&](double z) {
+    if (!(z > 0.0)) return 0.0;
+    const int panels = std::max(1, static_cast<int>(std::ceil(z / 0.5)));
+    const double hw = z / panels / 2.0;
+    double s = 0.0;
+    for (int p = 0; p < panels; ++p) {
+      const double mid = (2 * p + 1) * hw;
+      for (size_t k = 0; k < gx.size(); ++k) {
+        const double zz = mid + hw * gx[k];
+        s += gw[k] / std::sqrt(om * std::pow(1.0 + zz, 3) + ol);
+      }
+    }
+    return c_over_100 * s * hw;
+  };
+  for (int64_t i = 0; i < n; ++i) {
+    const double ra = in[4 * i] * deg, dec = in[4 * i + 1] * deg, z = in[4 * i + 2], w = in[4 * i + 3];
+    const double d = dist(z);
+    out[4 * i] = d * std::cos(dec) * std::cos(ra);
+    out[4 * i + 1] = d * std::cos(dec) * std::sin(ra);
+    out[4 * i + 2] = d * std::sin(dec);
+    out[4 * i + 3] = w;
+  }
+  return NCORR_OK;
 }
 
 int ncorr_logspace(double start, double end, int n, double* out) {

@@ -48,6 +48,8 @@ struct Geom {
   // FP32 error model: |v - V| <= ka*v + kb for every FP32 r^2 estimate v of
   // the reference's double r^2 V (pair and triangle stage alike).
   float ka, kb;
+  // Prefilter of the pair stage on cell-local FP32 estimates.
+  float pre_lo, pre_hi;
   // Heron margin: a candidate triangle is certainly accepted by the
   // reference's FP32 sqrtf test when H > S*(ha*S + hb), S = a+b+c.
   float ha, hb;

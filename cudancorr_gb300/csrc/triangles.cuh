@@ -5,13 +5,15 @@
 // One CTA of 256 threads owns one anchor (a point of catalogue 1) at a time;
 // anchors come from a global counter, in cell order.
 //  Phase A  the 27 (cell, image) slots around the anchor's home cell are
-//           streamed from the cell list; each candidate's r1^2 is estimated in
-//           FP32 from cell-local coordinates and classified against the bins
+//           streamed from the cell list. A cell-local FP32 estimate of r1^2
+//           drops candidates certainly out of range; for the others the
+//           anchor-relative offset is formed exactly in FP64 and rounded once
+//           to FP32, and r1^2 from it is classified against the bins
 //           (rigorous error band; the rare undecided ones are recomputed in
 //           FP64 exactly as the reference computes them). In-range neighbours
 //           go to a list in shared memory (overflow: a per-CTA global slab):
-//           anchor-relative offset d (float3), r1^2 estimate, exact bin,
-//           slot, point index, weight.
+//           offset d (float3), r1^2 estimate, exact bin, slot, point index,
+//           weight.
 //  Phase B  every neighbour pair (j, l) of the list(s) is a candidate
 //           triangle. The list is cut into 128-entry tiles; a warp holds one
 //           tile of l-entries in registers (4 per lane) and streams the
@@ -298,27 +300,36 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
           while (item >= pre[s + 1]) ++s;
           const int j = st[s] + (item - pre[s]);
           const float4 q = cat.pq[j];
-          const float dx = (q.x - qa.x) + s_do[s][0];
-          const float dy = (q.y - qa.y) + s_do[s][1];
-          const float dz = (q.z - qa.z) + s_do[s][2];
-          const float v = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-          unsigned code = table_code(v, tab, g.tab_scale, g.tab_n);
-          if (code == kCodeCareful) code = careful_code(v, s_e2lo, s_e2hi, nb, g.ka, g.kb);
-          if (code == kCodeExact) {
-            ++n_exact_pair;
+          // Cell-local FP32 prefilter: skip candidates certainly out of range.
+          const float fx = (q.x - qa.x) + s_do[s][0];
+          const float fy = (q.y - qa.y) + s_do[s][1];
+          const float fz = (q.z - qa.z) + s_do[s][2];
+          const float vp = fmaf(fz, fz, fmaf(fy, fy, fx * fx));
+          if (vp < g.pre_hi && vp > g.pre_lo) {
+            // Exact anchor-relative offset of the image (FP64), rounded once.
             const double4_16a p = cat.pd[j];
-            const double r = sqr_sep_exact(pa.x, pa.y, pa.z, __dadd_rn(p.x, s_shift[s][0]),
-                                           __dadd_rn(p.y, s_shift[s][1]), __dadd_rn(p.z, s_shift[s][2]),
-                                           g.fma_pattern);
-            code = (r < g.sqr_rmax && r > g.sqr_rmin) ? static_cast<unsigned>(exact_bin(r, s_sqr_bins, nb))
-                                                      : kCodeReject;
-          }
-          if (code < static_cast<unsigned>(nb)) {
-            acc = true;
-            ent = make_float4(dx, dy, dz, v);
-            meta = code | (static_cast<unsigned>(s) << 8);
-            pidx = j;
-            w = q.w;
+            const double Dx = __dsub_rn(__dadd_rn(p.x, s_shift[s][0]), pa.x);
+            const double Dy = __dsub_rn(__dadd_rn(p.y, s_shift[s][1]), pa.y);
+            const double Dz = __dsub_rn(__dadd_rn(p.z, s_shift[s][2]), pa.z);
+            const float dx = __double2float_rn(Dx), dy = __double2float_rn(Dy), dz = __double2float_rn(Dz);
+            const float v = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+            unsigned code = table_code(v, tab, g.tab_scale, g.tab_n);
+            if (code == kCodeCareful) code = careful_code(v, s_e2lo, s_e2hi, nb, g.ka, g.kb);
+            if (code == kCodeExact) {
+              ++n_exact_pair;
+              const double r = sqr_sep_exact(pa.x, pa.y, pa.z, __dadd_rn(p.x, s_shift[s][0]),
+                                             __dadd_rn(p.y, s_shift[s][1]), __dadd_rn(p.z, s_shift[s][2]),
+                                             g.fma_pattern);
+              code = (r < g.sqr_rmax && r > g.sqr_rmin) ? static_cast<unsigned>(exact_bin(r, s_sqr_bins, nb))
+                                                        : kCodeReject;
+            }
+            if (code < static_cast<unsigned>(nb)) {
+              acc = true;
+              ent = make_float4(dx, dy, dz, v);
+              meta = code | (static_cast<unsigned>(s) << 8);
+              pidx = j;
+              w = q.w;
+            }
           }
         }
         const unsigned bal = __ballot_sync(FULL, acc);

@@ -76,9 +76,17 @@ __global__ void k_fold(const unsigned long long* __restrict__ counts,
     if (dup) continue;
     seen[ns++] = key;
     if (weighted) {
-      long long whi = static_cast<long long>(wsum[2 * key + 1]);
-      unsigned long long wlo = wsum[2 * key];
-      acc += (static_cast<double>(whi) * 18446744073709551616.0 + static_cast<double>(wlo)) * inv_scale;
+      // Signed 128-bit (hi, lo) to double: negate negative values in integer
+      // arithmetic first, so the conversion never cancels.
+      unsigned long long lo = wsum[2 * key];
+      unsigned long long hi = wsum[2 * key + 1];
+      const bool neg = static_cast<long long>(hi) < 0;
+      if (neg) {
+        lo = ~lo + 1ull;
+        hi = ~hi + (lo == 0ull ? 1ull : 0ull);
+      }
+      const double mag = static_cast<double>(hi) * 18446744073709551616.0 + static_cast<double>(lo);
+      acc += (neg ? -mag : mag) * inv_scale;
     } else {
       cnt += counts[key];
     }

@@ -137,6 +137,13 @@ int survey_prep_cat(double* cat, int64_t n, double box[3], double ori[3]);
 int survey_prep_cat2(double* cat1, int64_t n1, double* cat2, int64_t n2, double box[3],
                      double ori[3]);
 
+/* survey::convert_coordinates (include/survey.hpp:20, source/survey.cu:39-57):
+ * rows (RA deg, Dec deg, redshift z, w) -> (x, y, z, w) with comoving distance
+ * d(z) = (c/100) * integral_0^z dz' / sqrt(OmegaM (1+z')^3 + OmegaLambda)
+ * in Mpc/h (source/survey.cu:17-37; H0 is unused there and here).
+ * cosmo = {H0, OmegaM, OmegaLambda}. in and out may alias. */
+int survey_convert_coordinates(const double cosmo[3], const double* in, int64_t n, double* out);
+
 /* logspace(start, end, n) (include/utils.hpp:9, source/utils.cu:16-27):
  * n log-spaced bin edges from start to end. */
 int ncorr_logspace(double start, double end, int n, double* out);

@@ -44,7 +44,8 @@ namespace {
 enum SqrSepPattern {
   kNoFma = 0,        // (dx*dx + dy*dy) + dz*dz, every operation rounded
   kFmaInnerDy = 1,   // fma(dz,dz, fma(dy,dy, dx*dx))
-  kFmaInnerDx = 2,   // fma(dz,dz, fma(dx,dx, dy*dy))
+  kFmaInnerDx = 2,   // fma(dz,dz, fma(dx,dx, dy*dy)): what nvcc emits for the
+                     // reference (pinned by the fma_probe fixture)
   kFmaOuterOnly = 3, // fma(dz,dz, dx*dx + dy*dy)
   kFmaInnerDyOnly = 4, // fma(dy,dy, dx*dx) + dz*dz
   kFmaInnerDxOnly = 5, // fma(dx,dx, dy*dy) + dz*dz

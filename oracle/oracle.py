@@ -19,9 +19,10 @@ RUNNER = HERE / "_build" / "libref_runner.so"
 REF_CUBIN = HERE / "_ref" / "reference_device.cubin"
 
 # Contraction of the reference's sqrSep under nvcc (pattern numbering of
-# ncorr_oracle.cpp): fma(dz, dz, fma(dy, dy, dx*dx)). Pinned by
-# tests/test_gpu_reference.py::test_fma_pattern against the reference kernel.
-FMA_PATTERN = 1
+# ncorr_oracle.cpp): fma(dz, dz, fma(dx, dx, dy*dy)). Pinned against the
+# reference kernel by tests/test_gpu_reference.py::test_fma_pattern and, on
+# CPU, by the recorded fma_probe fixture in tests/golden/.
+FMA_PATTERN = 2
 
 _D = ctypes.POINTER(ctypes.c_double)
 _lib = None
