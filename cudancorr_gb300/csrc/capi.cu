@@ -19,9 +19,9 @@ void launch_scan(const int* count, int ncell, int* start, int* cursor, cudaStrea
 void launch_scatter(const double4_16a* in, int n, const Geom& g, const int* cid, int* cursor,
                     double4_16a* pd, float4* pq, int* pc, cudaStream_t st);
 void launch_nbr_bound(const int* count, const Geom& g, int* out, cudaStream_t st);
-cudaError_t launch_triangles(const KArgs& a, bool survey, bool sym, bool weighted, int grid,
+cudaError_t launch_triangles(const KArgs& a, bool survey, bool sym, bool weighted, bool hg, int grid,
                              size_t smem, cudaStream_t st);
-int triangles_occupancy(bool survey, bool sym, bool weighted, size_t smem);
+int triangles_occupancy(bool survey, bool sym, bool weighted, bool hg, size_t smem);
 void launch_fold(const unsigned long long* counts, const unsigned long long* wsum, int nb,
                  bool weighted, double factor, double inv_scale, double* out,
                  unsigned long long* total, cudaStream_t st);
@@ -43,8 +43,10 @@ int fail(int code, const std::string& msg) {
 // separate the candidates: fma(dz, dz, fma(dx, dx, dy*dy)).
 constexpr int kDefaultFmaPattern = 2;
 
-// Budget of dynamic shared memory per CTA so that two CTAs share an SM.
+// Budget of dynamic shared memory per CTA so that two CTAs share an SM, and
+// the largest CTA histogram kept in shared memory.
 constexpr int kSmemBudget = 110 * 1024;
+constexpr long kHistSmemMax = 56 * 1024;
 
 struct DevBuf {
   void* p = nullptr;
@@ -86,6 +88,7 @@ struct ncorr_handle {
   long ncell = 0;
   Geom g;
   std::vector<unsigned char> table;
+  int table_scale = 0;  // code scale the uploaded table was built with
   std::vector<double> counts_all, counts_out, tri_bins_out;
   ncorr_stats stats;
   int device = 0;
@@ -143,9 +146,10 @@ void set_error_model(Geom& g) {
 }
 
 // Bin table: entry i covers every v with rint(v * scale) == i. Its code is the
-// bin that contains the whole error band of every such v, kCodeReject when
-// the band lies outside (rmin^2, rmax^2), or kCodeCareful otherwise.
-void build_table(Geom& g, std::vector<unsigned char>& tab) {
+// bin that contains the whole error band of every such v (times code_scale,
+// the byte stride of a bin in the CTA histogram), kCodeReject when the band
+// lies outside (rmin^2, rmax^2), or kCodeCareful otherwise.
+void build_table(Geom& g, int code_scale, std::vector<unsigned char>& tab) {
   const int n = kTableSize;
   tab.assign(n, static_cast<unsigned char>(kCodeCareful));
   const double vmax = g.sqr_rmax * 1.05;
@@ -167,7 +171,7 @@ void build_table(Geom& g, std::vector<unsigned char>& tab) {
     } else if (blo > g.sqr_rmin && bhi < g.sqr_rmax) {
       for (int b = 0; b < g.nb; ++b) {
         if (g.sqr_bins[b] <= blo && bhi < g.sqr_bins[b + 1]) {
-          code = static_cast<unsigned char>(b);
+          code = static_cast<unsigned char>(b * code_scale);
           break;
         }
       }
@@ -236,6 +240,7 @@ void compact(ncorr_handle* h) {
 int run(ncorr_handle* h, const double4_16a* d1, int n1, const double4_16a* d2, int n2, const double4_16a* d3,
         int n3, cudaStream_t st, const void* key1, const void* key2, const void* key3) {
   auto t0 = std::chrono::steady_clock::now();
+  cudaGetLastError();  // clear any error left by an earlier failed call
   // Distinct catalogues: identical inputs are gridded once.
   int role[3];
   role[0] = 0;
@@ -261,11 +266,6 @@ int run(ncorr_handle* h, const double4_16a* d1, int n1, const double4_16a* d2, i
   CU(cudaMemsetAsync(h->d_bound.p, 0, 2 * sizeof(int), st));
   CU(cudaMemsetAsync(h->d_stats.p, 0, 8 * sizeof(unsigned long long), st));
   CU(cudaMemsetAsync(h->d_total.p, 0, sizeof(unsigned long long), st));
-  if (!h->table_uploaded) {
-    CU(h->d_table.ensure(h->table.size()));
-    CU(cudaMemcpyAsync(h->d_table.p, h->table.data(), h->table.size(), cudaMemcpyHostToDevice, st));
-    h->table_uploaded = true;
-  }
 
   CU(cudaEventRecord(h->ev[0], st));
   bool done[3] = {false, false, false};
@@ -313,19 +313,42 @@ int run(ncorr_handle* h, const double4_16a* d1, int n1, const double4_16a* d2, i
     wscale = static_cast<float>(std::ldexp(1.0, e));
   }
 
-  // Shared-memory list capacity and overflow slabs.
+  // Count each triangle once for all six orderings when the three catalogues
+  // are one and the geometry makes every triangle's vertices see each other
+  // through bit-identical differences: survey mode, or a box divided exactly
+  // into >= 4 cells per axis; plus every point exactly inside its cell and,
+  // in a box, exact +-box images (kFlagNoSym6).
+  bool sym6 = sym && role[0] == role[1] && !(flags[role[0]] & kFlagNoSym6);
+  if (sym6 && !h->survey)
+    for (int d = 0; d < 3; ++d)
+      if (h->g.nc[d] < 4 || __builtin_fma(-static_cast<double>(h->g.nc[d]), h->g.cell, h->box[d]) != 0.0)
+        sym6 = false;
+
+  // CTA histogram in shared memory when it fits; a bin's byte stride is
+  // encoded in the table codes (u8, so at most 0xFD).
   const int nbin = h->nb * h->nb * h->nb;
+  const int elem = weighted ? 8 : 4;
+  bool hg = static_cast<long>(nbin) * elem > kHistSmemMax || h->nb * elem > 0xFD;
+  const int code_scale = hg ? 1 : elem;
+  if (h->table_scale != code_scale) {
+    build_table(h->g, code_scale, h->table);
+    CU(h->d_table.ensure(h->table.size()));
+    CU(cudaMemcpyAsync(h->d_table.p, h->table.data(), h->table.size(), cudaMemcpyHostToDevice, st));
+    h->table_scale = code_scale;
+  }
+
+  // Shared-memory list capacity and overflow slabs.
   int ks = 0;
   {
-    SmemLayout L0 = make_layout(h->nb, 0, sym, weighted);
+    SmemLayout L0 = make_layout(h->nb, 0, sym, weighted, hg);
     int per = (sym ? 1 : 2) * (16 + 4 + 4 + (weighted ? 4 : 0));
     ks = (kSmemBudget - L0.total) / per;
     ks = (ks / kTile) * kTile;
     if (ks < kTile) ks = kTile;
   }
-  SmemLayout L = make_layout(h->nb, ks, sym, weighted);
+  SmemLayout L = make_layout(h->nb, ks, sym, weighted, hg);
   const size_t smem = static_cast<size_t>(L.total);
-  int occ = triangles_occupancy(h->survey != 0, sym, weighted, smem);
+  int occ = triangles_occupancy(h->survey != 0, sym, weighted, hg, smem);
   if (occ <= 0) return fail(NCORR_ERR_CUDA, "triangle kernel does not fit on the device");
   int nsm = 0;
   CU(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->device));
@@ -361,13 +384,15 @@ int run(ncorr_handle* h, const double4_16a* d1, int n1, const double4_16a* d2, i
   a.slab_w = weighted ? h->slab_w.as<float>() : nullptr;
   a.ks = ks;
   a.kg = kg;
+  a.sym6 = sym6 ? 1 : 0;
+  a.code_scale = code_scale;
   a.wscale = wscale;
   a.stats = h->d_stats.as<unsigned long long>();
 
   CU(cudaEventRecord(h->ev[2], st));
-  if (n1 > 0) CU(launch_triangles(a, h->survey != 0, sym, weighted, grid, smem, st));
+  if (n1 > 0) CU(launch_triangles(a, h->survey != 0, sym, weighted, hg, grid, smem, st));
   CU(cudaEventRecord(h->ev[3], st));
-  launch_fold(a.hist.counts, a.hist.wsum, h->nb, weighted, sym ? 2.0 : 1.0, 1.0 / wscale,
+  launch_fold(a.hist.counts, a.hist.wsum, h->nb, weighted, sym6 ? 6.0 : (sym ? 2.0 : 1.0), 1.0 / wscale,
               h->d_out.as<double>(), h->d_total.as<unsigned long long>(), st);
   CU(cudaGetLastError());
   h->counts_all.assign(nbin, 0.0);
@@ -402,7 +427,7 @@ int run(ncorr_handle* h, const double4_16a* d1, int n1, const double4_16a* d2, i
   s.n_pair_evals = st_host[4];
   s.triangles = weighted ? 0 : total;
   s.weighted = weighted ? 1 : 0;
-  s.symmetric = sym ? 1 : 0;
+  s.symmetric = sym6 ? 6 : (sym ? 2 : 1);
   s.grid_ctas = grid;
   s.list_capacity = ks;
   return NCORR_OK;
@@ -476,7 +501,6 @@ int ncorr_create(const double box[3], int bin_type, const double* edges, int n_e
     g.e2hi[i] = f32_up(g.sqr_bins[i]);
   }
   set_error_model(g);
-  build_table(g, h->table);
   // Bin mids and the compacted (r1,r2,r3) table (source/cudaNcorr.cu:145-154).
   for (int i = 0; i < h->nb; ++i)
     for (int j = i; j < h->nb; ++j)

@@ -18,6 +18,32 @@ __device__ __forceinline__ bool axis_cell(double x, double cell, int* out) {
   return true;
 }
 
+// True when the point lies exactly inside its cell [c*cell, (c+1)*cell)
+// (the clamped face point x == nc*cell included) and, in box mode, its +-box
+// images are exact in FP64. When every point passes and cells are exactly
+// r_max wide, every pair closer than r_max is in adjacent cells and every
+// triangle's three vertices see each other through bit-identical
+// differences, which is what counting i < j < l once for all six orderings
+// needs.
+__device__ __forceinline__ bool sym6_point_ok(double x, int c, int d, const Geom& g) {
+  const double lo = __fma_rn(-static_cast<double>(c), g.cell, x);
+  const double hi = __fma_rn(-static_cast<double>(c + 1), g.cell, x);
+  if (!(lo >= 0.0)) return false;
+  if (!(hi < 0.0 || (hi == 0.0 && c == g.nc[d] - 1))) return false;
+  if (!g.survey) {
+    // Two-sum errors of x + box and x - box must vanish.
+    const double L = g.box[d];
+    const double s1 = __dadd_rn(x, L);
+    const double b1 = __dsub_rn(s1, x);
+    const double e1 = __dadd_rn(__dsub_rn(x, __dsub_rn(s1, b1)), __dsub_rn(L, b1));
+    const double s2 = __dsub_rn(x, L);
+    const double b2 = __dsub_rn(s2, x);
+    const double e2 = __dadd_rn(__dsub_rn(x, __dsub_rn(s2, b2)), __dsub_rn(-L, b2));
+    if (e1 != 0.0 || e2 != 0.0) return false;
+  }
+  return true;
+}
+
 // Per point: reference cell, validation, per-cell counts, weight summary.
 __global__ void k_assign(const double4_16a* __restrict__ in, int n, Geom g, int* __restrict__ cid,
                          int* __restrict__ count, int* __restrict__ flags,
@@ -42,6 +68,7 @@ __global__ void k_assign(const double4_16a* __restrict__ in, int n, Geom g, int*
       if (c == g.nc[d]) --c;
       if (c < 0 || c >= g.nc[d]) f |= kFlagOutOfGrid;
       ijk[d] = c;
+      if (!sym6_point_ok(c3[d], c, d, g)) f |= kFlagNoSym6;
     }
     if (p.w != 1.0) f |= kFlagWeighted;
     const float aw = fabsf(static_cast<float>(p.w));

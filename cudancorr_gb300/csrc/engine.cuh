@@ -33,6 +33,7 @@ constexpr int kFlagNonFinite = 2;
 constexpr int kFlagSurveyFace = 4;    // survey anchor whose unclamped cell index is nc
 constexpr int kFlagListOverflow = 8;  // neighbour list exceeded its slab (host bug)
 constexpr int kFlagWeighted = 16;     // some weight != 1.0 (informational)
+constexpr int kFlagNoSym6 = 32;       // a point near a cell face or with an inexact +-box image
 
 struct Geom {
   int nb;                 // bins per side

@@ -3,54 +3,69 @@
 
 namespace ncorr_gb300 {
 
-template <bool SV, bool SYM, bool W>
+template <bool SV, bool SYM, bool W, bool HG>
 static cudaError_t launch_one(const KArgs& a, int grid, size_t smem, cudaStream_t st) {
-  cudaError_t e = cudaFuncSetAttribute(k_triangles<SV, SYM, W>,
+  cudaError_t e = cudaFuncSetAttribute(k_triangles<SV, SYM, W, HG>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        static_cast<int>(smem));
   if (e != cudaSuccess) return e;
-  k_triangles<SV, SYM, W><<<grid, kThreads, smem, st>>>(a);
+  k_triangles<SV, SYM, W, HG><<<grid, kThreads, smem, st>>>(a);
   return cudaGetLastError();
 }
 
-template <bool SV, bool SYM, bool W>
+template <bool SV, bool SYM, bool W, bool HG>
 static int occupancy_one(size_t smem) {
-  cudaFuncSetAttribute(k_triangles<SV, SYM, W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       static_cast<int>(smem));
-  int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_triangles<SV, SYM, W>, kThreads, smem) !=
-      cudaSuccess)
+  if (cudaFuncSetAttribute(k_triangles<SV, SYM, W, HG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           static_cast<int>(smem)) != cudaSuccess) {
+    cudaGetLastError();
     return 0;
+  }
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_triangles<SV, SYM, W, HG>, kThreads, smem) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
   return n;
 }
 
-cudaError_t launch_triangles(const KArgs& a, bool survey, bool sym, bool weighted, int grid,
-                             size_t smem, cudaStream_t st) {
-  if (survey) {
-    if (sym) return weighted ? launch_one<true, true, true>(a, grid, smem, st)
-                             : launch_one<true, true, false>(a, grid, smem, st);
-    return weighted ? launch_one<true, false, true>(a, grid, smem, st)
-                    : launch_one<true, false, false>(a, grid, smem, st);
-  }
-  if (sym) return weighted ? launch_one<false, true, true>(a, grid, smem, st)
-                           : launch_one<false, true, false>(a, grid, smem, st);
-  return weighted ? launch_one<false, false, true>(a, grid, smem, st)
-                  : launch_one<false, false, false>(a, grid, smem, st);
+template <bool SV, bool SYM, bool W>
+static cudaError_t launch_hg(const KArgs& a, bool hg, int grid, size_t smem, cudaStream_t st) {
+  return hg ? launch_one<SV, SYM, W, true>(a, grid, smem, st) : launch_one<SV, SYM, W, false>(a, grid, smem, st);
 }
 
-int triangles_occupancy(bool survey, bool sym, bool weighted, size_t smem) {
+template <bool SV, bool SYM, bool W>
+static int occupancy_hg(bool hg, size_t smem) {
+  return hg ? occupancy_one<SV, SYM, W, true>(smem) : occupancy_one<SV, SYM, W, false>(smem);
+}
+
+cudaError_t launch_triangles(const KArgs& a, bool survey, bool sym, bool weighted, bool hg, int grid,
+                             size_t smem, cudaStream_t st) {
   if (survey) {
-    if (sym) return weighted ? occupancy_one<true, true, true>(smem) : occupancy_one<true, true, false>(smem);
-    return weighted ? occupancy_one<true, false, true>(smem) : occupancy_one<true, false, false>(smem);
+    if (sym) return weighted ? launch_hg<true, true, true>(a, hg, grid, smem, st)
+                             : launch_hg<true, true, false>(a, hg, grid, smem, st);
+    return weighted ? launch_hg<true, false, true>(a, hg, grid, smem, st)
+                    : launch_hg<true, false, false>(a, hg, grid, smem, st);
   }
-  if (sym) return weighted ? occupancy_one<false, true, true>(smem) : occupancy_one<false, true, false>(smem);
-  return weighted ? occupancy_one<false, false, true>(smem) : occupancy_one<false, false, false>(smem);
+  if (sym) return weighted ? launch_hg<false, true, true>(a, hg, grid, smem, st)
+                           : launch_hg<false, true, false>(a, hg, grid, smem, st);
+  return weighted ? launch_hg<false, false, true>(a, hg, grid, smem, st)
+                  : launch_hg<false, false, false>(a, hg, grid, smem, st);
+}
+
+int triangles_occupancy(bool survey, bool sym, bool weighted, bool hg, size_t smem) {
+  if (survey) {
+    if (sym) return weighted ? occupancy_hg<true, true, true>(hg, smem) : occupancy_hg<true, true, false>(hg, smem);
+    return weighted ? occupancy_hg<true, false, true>(hg, smem) : occupancy_hg<true, false, false>(hg, smem);
+  }
+  if (sym) return weighted ? occupancy_hg<false, true, true>(hg, smem) : occupancy_hg<false, true, false>(hg, smem);
+  return weighted ? occupancy_hg<false, false, true>(hg, smem) : occupancy_hg<false, false, false>(hg, smem);
 }
 
 // Folds the unsorted (bin_j, bin_l, bin_3) histogram into the reference's
 // triCountsAll_ layout: out[hi + mid*nb + lo*nb^2] for lo <= mid <= hi sums
 // the distinct permutations in a fixed order (deterministic), times `factor`
-// (2 when only pairs j < l were visited).
+// (2 when only pairs j < l were visited, 6 when only i < j < l).
 __global__ void k_fold(const unsigned long long* __restrict__ counts,
                        const unsigned long long* __restrict__ wsum, int nb, int weighted,
                        double factor, double inv_scale, double* __restrict__ out,

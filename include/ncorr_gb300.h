@@ -57,7 +57,9 @@ typedef struct ncorr_stats {
   uint64_t n_exact_tris;   /* triangles settled by the FP64 path */
   uint64_t triangles;      /* sum of the full histogram (count mode) */
   int weighted;            /* 1: some weight != 1.0 (fixed-point weighted sums) */
-  int symmetric;           /* 1: catalogues 2 and 3 identical (pairs j<l, x2) */
+  int symmetric;           /* orderings each visited triangle stands for: 1 (all (j,l)),
+                              2 (p2 == p3: pairs j<l), 6 (p1 == p2 == p3 in a geometry
+                              where all three vertices see each other identically) */
   int grid_ctas;           /* persistent CTAs of the triangle kernel */
   int list_capacity;       /* shared-memory neighbour-list capacity */
 } ncorr_stats;

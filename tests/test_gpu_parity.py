@@ -54,14 +54,21 @@ def test_box_uniform_20k(engine_lib, oracle):
     assert ref.sum() > 1e6 - 1e5
 
 
-def test_asymmetric_path_equals_symmetric(engine_lib, oracle):
-    """p3 a copy of p2 (distinct array) forces the full (j, l) double loop; it
-    must reproduce the j<l x2 result bit for bit."""
-    p, box, edges = cases.small_box_clustered()
-    h_sym, _, st_sym = run_engine(box, edges, p, p, p)
-    h_asym, _, st_asym = run_engine(box, edges, p, p, p.copy())
-    assert st_sym["symmetric"] == 1 and st_asym["symmetric"] == 0
-    assert np.array_equal(h_sym, h_asym)
+@pytest.mark.parametrize("make", [cases.small_box_clustered, cases.small_box_uniform,
+                                  cases.small_box_nondivisible], ids=lambda f: f.__name__)
+def test_symmetry_modes_agree(engine_lib, oracle, make):
+    """The three loop forms give the same histogram bit for bit: all (j, l)
+    (p3 a distinct copy), pairs j<l x2 (p1 a distinct copy), and -- where the
+    geometry allows it -- i<j<l x6 (one catalogue for all three)."""
+    p, box, edges = make()
+    h6, _, st6 = run_engine(box, edges, p, p, p)
+    h2, _, st2 = run_engine(box, edges, p.copy(), p, p)
+    h1, _, st1 = run_engine(box, edges, p, p, p.copy())
+    assert st2["symmetric"] == 2 and st1["symmetric"] == 1
+    divisible = make is not cases.small_box_nondivisible
+    assert st6["symmetric"] == (6 if divisible else 2)
+    assert np.array_equal(h6, h2) and np.array_equal(h2, h1)
+    assert np.array_equal(h6, oracle.count_threeD(box, edges, p))
 
 
 def test_cross_catalogue_box(engine_lib, oracle):
@@ -109,6 +116,22 @@ def test_weighted_box_with_negative_weights(engine_lib, oracle):
     scale = oracle.count_threeD(box, edges, np.abs(p))
     nz = scale != 0
     assert np.max(np.abs(h[nz] - ref[nz]) / scale[nz]) < WEIGHTED_RTOL
+
+
+def test_many_bins_global_histogram(engine_lib, oracle):
+    """Bin counts whose histogram does not fit in shared memory (63 bins
+    unweighted, 40 weighted) take the global-histogram path."""
+    p, box, edges = cases.small_box_uniform(n=2500)
+    e63 = C.linear_edges(30.0, 63)
+    h, _, _ = run_engine(box, e63, p)
+    assert np.array_equal(h, oracle.count_threeD(box, e63, p))
+    d, r, sbox, ori, _ = cases.small_survey(nd=1500, nr=3000, weighted=True)
+    e40 = oracle.logspace(5.0, 120.0, 41)
+    h, _, _ = run_engine(sbox, e40, d, d, r, survey=True, ori=ori)
+    ref = oracle.count_threeD(sbox, e40, d, d, r, survey=True)
+    nz = ref != 0
+    assert np.array_equal(h != 0, nz)
+    assert np.max(np.abs(h[nz] - ref[nz]) / np.abs(ref[nz])) < WEIGHTED_RTOL
 
 
 def test_empty_and_single(engine_lib):
