@@ -271,7 +271,8 @@ def run_engine(args) -> dict:
                                    "(MEASURED_PEAKS.json has no FP32 entry)"},
         "gpu_launches": 6 * args.steps,
         "clocks": clocks,
-        "exact_path": {"pairs": int(st_last["n_exact_pairs"]), "triangles": int(st_last["n_exact_tris"])},
+        "exact_path": {"pairs": int(st_last["n_exact_pairs"]), "triangles": int(st_last["n_exact_tris"]),
+                       "flagged_rows": int(st_last["n_flagged_rows"]), "queued": int(st_last["n_queued"])},
     }
     if world == 1 and not args.no_cpu_baseline and args.anchor_slab is None:
         out["cpu_baseline"] = cpu_baseline(p, box, edges)

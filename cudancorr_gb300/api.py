@@ -57,7 +57,8 @@ class NcorrStats(ctypes.Structure):
         ("ms_total", ctypes.c_double), ("n_anchors", ctypes.c_uint64),
         ("n_pair_evals", ctypes.c_uint64), ("n_pairs", ctypes.c_uint64),
         ("n_exact_pairs", ctypes.c_uint64), ("n_exact_tris", ctypes.c_uint64),
-        ("triangles", ctypes.c_uint64), ("weighted", ctypes.c_int), ("symmetric", ctypes.c_int),
+        ("triangles", ctypes.c_uint64), ("n_flagged_rows", ctypes.c_uint64), ("n_queued", ctypes.c_uint64),
+        ("weighted", ctypes.c_int), ("symmetric", ctypes.c_int),
         ("grid_ctas", ctypes.c_int), ("list_capacity", ctypes.c_int),
     ]
 
@@ -70,7 +71,10 @@ _D = ctypes.POINTER(ctypes.c_double)
 
 
 def library_path() -> pathlib.Path:
-    return _build.library_path()
+    """The engine library: NCORR_LIBRARY when set, else the in-tree build."""
+    import os
+    override = os.environ.get("NCORR_LIBRARY")
+    return pathlib.Path(override) if override else _build.library_path()
 
 
 def load_library() -> ctypes.CDLL:

@@ -34,9 +34,9 @@ def nvcc() -> str:
     raise RuntimeError("nvcc not found")
 
 
-def _compile(src: str, verbose: bool) -> pathlib.Path:
-    obj = OBJ / (pathlib.Path(src).stem + ".o")
-    cmd = [nvcc(), *GENCODE, *FLAGS, "-c", str(CSRC / src), "-o", str(obj)]
+def _compile(src: str, verbose: bool, obj_dir: pathlib.Path = None, defines=()) -> pathlib.Path:
+    obj = (obj_dir or OBJ) / (pathlib.Path(src).stem + ".o")
+    cmd = [nvcc(), *GENCODE, *FLAGS, *[f"-D{d}" for d in defines], "-c", str(CSRC / src), "-o", str(obj)]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -51,17 +51,22 @@ def library_path() -> pathlib.Path:
     return OUT / LIBNAME
 
 
-def build(verbose: bool = False, force: bool = False) -> pathlib.Path:
-    """Compiles (when stale) and returns the path of the shared library."""
-    OBJ.mkdir(parents=True, exist_ok=True)
-    lib = library_path()
+def build(verbose: bool = False, force: bool = False, out: pathlib.Path = None, defines=()) -> pathlib.Path:
+    """Compiles (when stale) and returns the path of the shared library.
+
+    `out` and `defines` build a variant of the library (tuning constants set
+    with -D) into another directory."""
+    out_dir = pathlib.Path(out) if out else OUT
+    obj_dir = out_dir / "obj"
+    obj_dir.mkdir(parents=True, exist_ok=True)
+    lib = out_dir / LIBNAME
     deps = [CSRC / s for s in SOURCES] + list(CSRC.glob("*.cuh")) + [ROOT / "include" / "ncorr_gb300.h"]
     if lib.exists() and not force:
         newest = max(p.stat().st_mtime for p in deps)
         if lib.stat().st_mtime >= newest:
             return lib
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        objs = list(ex.map(lambda s: _compile(s, verbose), SOURCES))
+        objs = list(ex.map(lambda s: _compile(s, verbose, obj_dir, defines), SOURCES))
     tmp = lib.with_suffix(".so.tmp")
     cmd = [nvcc(), *GENCODE, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <string>
@@ -22,6 +23,7 @@ void launch_nbr_bound(const int* count, const Geom& g, int* out, cudaStream_t st
 cudaError_t launch_triangles(const KArgs& a, bool survey, bool sym, bool weighted, bool hg, int grid,
                              size_t smem, cudaStream_t st);
 int triangles_occupancy(bool survey, bool sym, bool weighted, bool hg, size_t smem);
+void launch_exact(const KArgs& a, bool survey, bool weighted, int grid, cudaStream_t st);
 void launch_fold(const unsigned long long* counts, const unsigned long long* wsum, int nb,
                  bool weighted, double factor, double inv_scale, double* out,
                  unsigned long long* total, cudaStream_t st);
@@ -47,6 +49,7 @@ constexpr int kDefaultFmaPattern = 2;
 // the largest CTA histogram kept in shared memory.
 constexpr int kSmemBudget = 110 * 1024;
 constexpr long kHistSmemMax = 56 * 1024;
+constexpr unsigned kExactQueueCap = 1u << 24;  // 16M entries, 256 MiB
 
 struct DevBuf {
   void* p = nullptr;
@@ -97,6 +100,9 @@ struct ncorr_handle {
   CatDev cat[3];
   DevBuf d_table, d_flags, d_wmax, d_work, d_bound, d_hist, d_out, d_stats, d_total;
   DevBuf slab_e, slab_m, slab_p, slab_w;
+  DevBuf xq, xq_count;  // deferred exact candidates
+  DevBuf d_args;        // global copy of the triangle kernel's arguments
+  unsigned xq_cap = 0;
   bool table_uploaded = false;
 };
 
@@ -388,9 +394,21 @@ int run(ncorr_handle* h, const double4_16a* d1, int n1, const double4_16a* d2, i
   a.code_scale = code_scale;
   a.wscale = wscale;
   a.stats = h->d_stats.as<unsigned long long>();
+  // Deferred exact candidates: about one in 10^4 candidates at the clustered
+  // 2M-point workload; beyond the capacity they are settled in place.
+  CU(h->xq.ensure(static_cast<size_t>(std::max(h->xq_cap, 1u)) * sizeof(ExactEntry)));
+  CU(h->xq_count.ensure(sizeof(unsigned)));
+  CU(cudaMemsetAsync(h->xq_count.p, 0, sizeof(unsigned), st));
+  a.xq = h->xq.as<ExactEntry>();
+  a.xq_count = h->xq_count.as<unsigned>();
+  a.xq_cap = h->xq_cap;
 
+  CU(h->d_args.ensure(sizeof(KArgs)));
+  a.self = h->d_args.as<KArgs>();
+  CU(cudaMemcpyAsync(h->d_args.p, &a, sizeof(KArgs), cudaMemcpyHostToDevice, st));
   CU(cudaEventRecord(h->ev[2], st));
   if (n1 > 0) CU(launch_triangles(a, h->survey != 0, sym, weighted, hg, grid, smem, st));
+  if (n1 > 0) launch_exact(a, h->survey != 0, weighted, nsm * 4, st);
   CU(cudaEventRecord(h->ev[3], st));
   launch_fold(a.hist.counts, a.hist.wsum, h->nb, weighted, sym6 ? 6.0 : (sym ? 2.0 : 1.0), 1.0 / wscale,
               h->d_out.as<double>(), h->d_total.as<unsigned long long>(), st);
@@ -425,6 +443,8 @@ int run(ncorr_handle* h, const double4_16a* d1, int n1, const double4_16a* d2, i
   s.n_anchors = st_host[2];
   s.n_pairs = st_host[3];
   s.n_pair_evals = st_host[4];
+  s.n_flagged_rows = st_host[5];
+  s.n_queued = st_host[6];
   s.triangles = weighted ? 0 : total;
   s.weighted = weighted ? 1 : 0;
   s.symmetric = sym6 ? 6 : (sym ? 2 : 1);
@@ -513,6 +533,10 @@ int ncorr_create(const double box[3], int bin_type, const double* edges, int n_e
         }
   h->counts_all.assign(static_cast<size_t>(h->nb) * h->nb * h->nb, 0.0);
   std::memset(&h->stats, 0, sizeof(h->stats));
+  // Capacity of the deferred exact queue; NCORR_EXACT_QUEUE_CAP overrides it
+  // (0 settles every uncertain candidate in place).
+  h->xq_cap = kExactQueueCap;
+  if (const char* env = std::getenv("NCORR_EXACT_QUEUE_CAP")) h->xq_cap = static_cast<unsigned>(std::strtoul(env, nullptr, 10));
   cudaGetDevice(&h->device);
   cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
   for (int i = 0; i < 4 && e == cudaSuccess; ++i) e = cudaEventCreate(&h->ev[i]);
@@ -552,7 +576,7 @@ void ncorr_destroy(ncorr_handle* h) {
   }
   for (DevBuf* b : {&h->d_table, &h->d_flags, &h->d_wmax, &h->d_work, &h->d_bound, &h->d_hist,
                     &h->d_out, &h->d_stats, &h->d_total, &h->slab_e, &h->slab_m, &h->slab_p,
-                    &h->slab_w})
+                    &h->slab_w, &h->xq, &h->xq_count, &h->d_args})
     b->release();
   for (auto& e : h->ev)
     if (e) cudaEventDestroy(e);

@@ -20,8 +20,11 @@ constexpr int kThreads = 256;    // triangle kernel CTA
 constexpr int kWarps = kThreads / 32;
 constexpr int kReg = 4;          // list entries per lane held in registers
 constexpr int kTile = 32 * kReg; // tile edge of the pair loop
-constexpr int kQueueCap = 256;   // per-warp queue of exact-path candidates
-constexpr int kTableSize = 8192; // bin table entries (u8)
+constexpr int kQueueCap = 256;   // per-warp queue of careful/exact-path candidates
+#ifndef NCORR_TABLE_SIZE
+#define NCORR_TABLE_SIZE 32768
+#endif
+constexpr int kTableSize = NCORR_TABLE_SIZE;  // bin table entries (u8)
 
 // Bin codes returned by the FP32 classifiers.
 constexpr unsigned kCodeReject = 0xFEu;
@@ -66,6 +69,15 @@ struct Catalog {
   const int* start;
   const int* count;
   int n;
+};
+
+// A candidate triangle whose FP32 classification stays uncertain, deferred to
+// the exact FP64 kernel: anchor (sorted index in catalogue 1), the two
+// neighbours (sorted indices in catalogues 2 and 3), and
+// meta = slot_j | slot_l << 5 | bin_j << 10 | bin_l << 18.
+struct ExactEntry {
+  int ai, pj, pl;
+  unsigned meta;
 };
 
 // Fixed-point weighted sums are kept as signed 128-bit integers in two u64

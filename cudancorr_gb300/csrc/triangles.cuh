@@ -39,13 +39,18 @@
 namespace ncorr_gb300 {
 
 constexpr unsigned kCodeExact = 0xFDu;
+
+// j-rows evaluated per iteration of the unweighted pair loop (1 or 2).
+#ifndef NCORR_ROW_UNROLL
+#define NCORR_ROW_UNROLL 2
+#endif
 constexpr int kSubJ = 32;                       // j-entries per work item
 constexpr int kSubPerTile = kTile / kSubJ;      // work items per tile pair
 
 // Shared-memory layout (dynamic part). The bin table sits at offset 0 and the
 // CTA histogram right after it, so both are addressed with immediate offsets.
 struct SmemLayout {
-  int table, hist, e2, e3, m2, m3, p2, p3, w2, w3, queue, total;
+  int table, hist, e2, e3, m2, m3, p2, p3, w2, w3, queue, xbuf, scratch, total;
 };
 
 __host__ __device__ inline int align16(int x) { return (x + 15) & ~15; }
@@ -77,6 +82,10 @@ __host__ __device__ inline SmemLayout make_layout(int nb, int ks, bool sym, bool
   o = align16(o);
   L.queue = o;
   o += kWarps * kQueueCap * 8;
+  L.xbuf = o;  // per warp: 32 uncertain candidates awaiting the exact kernel
+  o += kWarps * 32 * 16;
+  L.scratch = o;  // one word per lane: sink of non-counting reductions
+  o += 32 * 4;
   L.total = align16(o);
   return L;
 }
@@ -100,7 +109,15 @@ struct KArgs {
   // Byte stride of one bin in the CTA histogram as encoded in the table
   // (4: u32 counts, 8: int64 sums, 1: global histogram, bins unscaled).
   int code_scale;
-  unsigned long long* stats;  // exact tris, exact pairs, anchors, W, P
+  unsigned long long* stats;  // exact tris, exact pairs, anchors, W, P, flagged rows, queued
+  // Deferred exact candidates (null: settle them in place).
+  ExactEntry* xq;
+  unsigned* xq_count;
+  unsigned xq_cap;
+  // A copy of these arguments in global memory, used by the out-of-line
+  // paths (taking the address of the kernel parameter would copy it to local
+  // memory in every thread).
+  const KArgs* self;
 };
 
 // Bin code of an FP32 r^2 estimate: table[rint(v * scale)], clamped.
@@ -175,6 +192,125 @@ __device__ __forceinline__ void red_shared_u64_if(unsigned addr, unsigned long l
       : "memory");
 }
 
+// One unweighted candidate (j, l) in hand-written PTX: the FP32 r3^2, its
+// table code, the Heron proof, the shared-memory histogram reduction, and the
+// flag "needs the careful/exact path". Every rounding is explicit (.rn),
+// matching the error model. kj/kl are byte offsets into the shared histogram
+// (kj includes its base address); `in` masks the candidate (diagonal tiles:
+// j < l). The reduction is unconditional: a candidate that does not count
+// adds to the lane's own scratch word `dummy` instead, which keeps the loop
+// free of the branch a predicated atomic compiles to.
+// Classification of one candidate, shared verbatim by the counting body and
+// the flag-only body so that both take bit-identical decisions.
+#define NCORR_CAND_CLASSIFY                    \
+  "sub.rn.f32 dx, %1, %6;\n\t"                 \
+  "sub.rn.f32 dy, %2, %7;\n\t"                 \
+  "sub.rn.f32 dz, %3, %8;\n\t"                 \
+  "mul.rn.f32 v, dx, dx;\n\t"                  \
+  "fma.rn.f32 v, dy, dy, v;\n\t"               \
+  "fma.rn.f32 v, dz, dz, v;\n\t"               \
+  "fma.rn.f32 y, v, %13, 0f4B000000;\n\t"      \
+  "mov.b32 ia, y;\n\t"                         \
+  "add.u32 ia, ia, %14;\n\t"                   \
+  "min.u32 ia, ia, %15;\n\t"                   \
+  "ld.shared.u8 code, [ia];\n\t"               \
+  "add.rn.f32 s, %4, %9;\n\t"                  \
+  "sub.rn.f32 t, v, s;\n\t"                    \
+  "neg.f32 nt, t;\n\t"                         \
+  "mul.rn.f32 p4, %5, %9;\n\t"                 \
+  "fma.rn.f32 H, nt, t, p4;\n\t"               \
+  "add.rn.f32 S, s, v;\n\t"                    \
+  "fma.rn.f32 qq, %17, S, %18;\n\t"            \
+  "mul.rn.f32 nd, S, qq;\n\t"                  \
+  "setp.gt.f32 cl, H, nd;\n\t"                 \
+  "setp.lt.u32 ok, code, %16;\n\t"             \
+  "setp.eq.u32 car, code, 255;\n\t"            \
+  NCORR_CAND_MASK                              \
+  "and.pred upd, ok, cl;\n\t"                  \
+  "not.pred ncl, cl;\n\t"                      \
+  "and.pred wq, ok, ncl;\n\t"                  \
+  "or.pred wq, wq, car;\n\t"                   \
+  "selp.u32 %0, 1, 0, wq;\n\t"
+
+// Diagonal tiles mask the candidate with `in` (operand 12).
+#define NCORR_CAND_MASK_ON           \
+  "setp.ne.u32 inp, %12, 0;\n\t"     \
+  "and.pred ok, ok, inp;\n\t"        \
+  "and.pred car, car, inp;\n\t"
+
+#define NCORR_CAND_DECLS                                         \
+  ".reg .f32 dx, dy, dz, v, y, s, t, nt, p4, H, S, qq, nd;\n\t" \
+  ".reg .b32 ia, code, key, adr;\n\t"                            \
+  ".reg .pred ok, cl, ncl, car, upd, wq, inp;\n\t"
+
+// One unweighted candidate (j, l) in hand-written PTX: the FP32 r3^2, its
+// table code, the Heron proof, the shared-memory histogram reduction, and the
+// flag "needs the careful/exact path". Every rounding is explicit (.rn),
+// matching the error model. kj/kl are byte offsets into the shared histogram
+// (kj includes its base address); `in` masks the candidate (diagonal tiles:
+// j < l). The reduction is unconditional: a candidate that does not count
+// adds to the lane's own scratch word `dummy` instead, which keeps the loop
+// free of the branch a predicated atomic compiles to.
+template <bool DIAG>
+__device__ __forceinline__ unsigned cand_count(float ex, float ey, float ez, float a, float a4, float lx,
+                                               float ly, float lz, float b, unsigned kj, unsigned kl,
+                                               unsigned in, float tscale, unsigned tab_adj,
+                                               unsigned tab_last, unsigned nb_cs, float ha, float hb,
+                                               unsigned dummy) {
+  unsigned q;
+#define NCORR_CAND_COUNT_ASM                                                                          \
+  asm volatile(                                                                                      \
+      "{\n\t" NCORR_CAND_DECLS NCORR_CAND_CLASSIFY                                                     \
+      "add.u32 key, %10, %11;\n\t"                                                                   \
+      "add.u32 key, key, code;\n\t"                                                                  \
+      "selp.b32 adr, key, %19, upd;\n\t"                                                             \
+      "red.shared.add.u32 [adr], 1;\n\t"                                                             \
+      "}"                                                                                            \
+      : "=r"(q)                                                                                      \
+      : "f"(ex), "f"(ey), "f"(ez), "f"(a), "f"(a4), "f"(lx), "f"(ly), "f"(lz), "f"(b), "r"(kj), "r"(kl), \
+        "r"(in), "f"(tscale), "r"(tab_adj), "r"(tab_last), "r"(nb_cs), "f"(ha), "f"(hb), "r"(dummy))
+  if (DIAG) {
+#define NCORR_CAND_MASK NCORR_CAND_MASK_ON
+    NCORR_CAND_COUNT_ASM;
+#undef NCORR_CAND_MASK
+  } else {
+#define NCORR_CAND_MASK ""
+    NCORR_CAND_COUNT_ASM;
+#undef NCORR_CAND_MASK
+  }
+#undef NCORR_CAND_COUNT_ASM
+  return q;
+}
+
+// The same classification without the histogram update: 1 when the
+// candidate needs the careful/exact path.
+__device__ __forceinline__ unsigned cand_flag(float ex, float ey, float ez, float a, float a4, float lx,
+                                              float ly, float lz, float b, unsigned in, float tscale,
+                                              unsigned tab_adj, unsigned tab_last, unsigned nb_cs, float ha,
+                                              float hb) {
+  unsigned q;
+#define NCORR_CAND_MASK NCORR_CAND_MASK_ON
+  asm volatile(
+      "{\n\t" NCORR_CAND_DECLS NCORR_CAND_CLASSIFY "}"
+      : "=r"(q)
+      : "f"(ex), "f"(ey), "f"(ez), "f"(a), "f"(a4), "f"(lx), "f"(ly), "f"(lz), "f"(b), "r"(0u), "r"(0u),
+        "r"(in), "f"(tscale), "r"(tab_adj), "r"(tab_last), "r"(nb_cs), "f"(ha), "f"(hb));
+#undef NCORR_CAND_MASK
+  return q;
+}
+
+__device__ __forceinline__ float4 lds_f4(unsigned addr) {
+  float4 v;
+  asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(addr));
+  return v;
+}
+
+__device__ __forceinline__ unsigned lds_u32(unsigned addr) {
+  unsigned v;
+  asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(addr));
+  return v;
+}
+
 // Histogram update. The key is the table-scaled code: a byte offset into the
 // shared histogram, or a plain bin index for the global histogram (HG).
 template <bool WEIGHTED, bool HG>
@@ -191,6 +327,196 @@ __device__ __forceinline__ void hist_add(unsigned char* hist_s, const KArgs& a, 
     else
       atomicAdd(reinterpret_cast<unsigned*>(hist_s + key), 1u);
   }
+}
+
+// Settles one uncertain candidate exactly as the reference computes it
+// (source/device.cu:154-201, :259-315 / :381-431): FP64 images and sides
+// with the pinned sqrSep contraction, FP32 sqrtf triangle test, bin search;
+// adds into the global unsorted histogram. Uses global data only.
+template <bool SURVEY, bool WEIGHTED>
+__device__ __forceinline__ void settle_exact(const KArgs& a, const ExactEntry& e) {
+  const Geom& g = a.g;
+  const int nb = g.nb;
+  const int sj = static_cast<int>(e.meta & 31u), sl = static_cast<int>((e.meta >> 5) & 31u);
+  const unsigned bj = (e.meta >> 10) & 0xffu, bl = (e.meta >> 18) & 0xffu;
+  const double4_16a pa = a.c1.pd[e.ai];
+  const int hc = a.c1.pc[e.ai];
+  const int h[3] = {hc / (g.nc[2] * g.nc[1]), (hc / g.nc[2]) % g.nc[1], hc % g.nc[2]};
+  double shj[3], shl[3];
+  // Image shift of a slot (source/device.cu:89-122); zero in survey mode.
+  const int dj3[3] = {sj / 9 - 1, (sj / 3) % 3 - 1, sj % 3 - 1};
+  const int dl3[3] = {sl / 9 - 1, (sl / 3) % 3 - 1, sl % 3 - 1};
+  for (int d = 0; d < 3; ++d) {
+    shj[d] = 0.0;
+    shl[d] = 0.0;
+    if (!SURVEY) {
+      const int cj = h[d] + dj3[d], cl = h[d] + dl3[d];
+      if (cj == g.nc[d]) shj[d] = g.box[d]; else if (cj == -1) shj[d] = -g.box[d];
+      if (cl == g.nc[d]) shl[d] = g.box[d]; else if (cl == -1) shl[d] = -g.box[d];
+    }
+  }
+  const double4_16a dj = a.c2.pd[e.pj];
+  const double4_16a dl = a.c3.pd[e.pl];
+  const double jx = __dadd_rn(dj.x, shj[0]), jy = __dadd_rn(dj.y, shj[1]), jz = __dadd_rn(dj.z, shj[2]);
+  const double lx = __dadd_rn(dl.x, shl[0]), ly = __dadd_rn(dl.y, shl[1]), lz = __dadd_rn(dl.z, shl[2]);
+  const double r1 = sqr_sep_exact(pa.x, pa.y, pa.z, jx, jy, jz, g.fma_pattern);
+  const double r2 = sqr_sep_exact(pa.x, pa.y, pa.z, lx, ly, lz, g.fma_pattern);
+  const double r3 = sqr_sep_exact(jx, jy, jz, lx, ly, lz, g.fma_pattern);
+  if (!(r3 < g.sqr_rmax && r3 > g.sqr_rmin) || !exact_triangle_ok(r1, r2, r3)) return;
+  int lo = 0, hi = nb - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (r3 >= g.sqr_bins[mid]) lo = mid; else hi = mid - 1;
+  }
+  const unsigned key = (bj * nb + bl) * nb + static_cast<unsigned>(lo);
+  if (WEIGHTED) {
+    const float w = (static_cast<float>(pa.w) * static_cast<float>(dj.w)) * static_cast<float>(dl.w) * a.wscale;
+    add128(&a.hist.wsum[2 * key], __float2ll_rn(w));
+  } else {
+    atomicAdd(&a.hist.counts[key], 1ull);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Rarely taken paths, kept out of line so that the hot pair loop stays small
+// in the instruction cache. Cold holds one warp's state for them.
+struct Cold {
+  const KArgs* a;
+  ListView l2, l3;
+  unsigned long long* queue;  // this warp's (j, l) queue
+  ExactEntry* xbuf;           // this warp's buffer of uncertain candidates
+  const float* e2lo;
+  const float* e2hi;
+  const double* sqr_bins;
+  unsigned char* tab;
+  unsigned char* hist_s;
+  int qn, xn;
+  int nb, cs, ai;
+  float wa;
+  unsigned lane, lt_mask;
+  unsigned long long n_exact_tri, n_queued, n_flag_rows;
+};
+
+// Moves the warp's buffered uncertain candidates to the global queue (one
+// atomic per 32), or settles them here when the queue is full.
+template <bool SURVEY, bool WEIGHTED>
+__device__ __noinline__ void cold_flush_exact(Cold& c) {
+  const KArgs& a = *c.a;
+  if (c.xn == 0) return;
+  unsigned base = 0;
+  if (c.lane == 0 && a.xq) base = atomicAdd(a.xq_count, static_cast<unsigned>(c.xn));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (static_cast<int>(c.lane) < c.xn) {
+    const ExactEntry e = c.xbuf[c.lane];
+    if (a.xq && base + c.lane < a.xq_cap)
+      a.xq[base + c.lane] = e;
+    else
+      settle_exact<SURVEY, WEIGHTED>(a, e);
+  }
+  c.xn = 0;
+  __syncwarp();
+}
+
+// Settles the queued candidates, 32 per round: the explicit FP32 band and the
+// Heron test decide most; the rest go to the exact buffer.
+template <bool SURVEY, bool WEIGHTED, bool HG>
+__device__ __noinline__ void cold_drain(Cold& c) {
+  const KArgs& a = *c.a;
+  const Geom& g = a.g;
+  const int nb = c.nb;
+  for (int q0 = 0; q0 < c.qn; q0 += 32) {
+    const int qi = q0 + static_cast<int>(c.lane);
+    bool exact = false;
+    ExactEntry xe;
+    if (qi < c.qn) {
+      const unsigned long long pr = c.queue[qi];
+      const int j = static_cast<int>(pr & 0xffffffffu);
+      const int l = static_cast<int>(pr >> 32);
+      const float4 ej = c.l2.E(j, a.ks);
+      const unsigned mj = c.l2.M(j, a.ks);
+      const float4 el = c.l3.E(l, a.ks);
+      const unsigned ml = c.l3.M(l, a.ks);
+      const float dx = ej.x - el.x, dy = ej.y - el.y, dz = ej.z - el.z;
+      const float v = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+      const unsigned key_jl = ((mj & 0xffu) * nb * nb + (ml & 0xffu) * nb);
+      unsigned code = careful_code(v, c.e2lo, c.e2hi, nb, g.ka, g.kb);
+      if (code < static_cast<unsigned>(nb)) {
+        const float s = ej.w + el.w, t = v - s;
+        const float H = fmaf(-t, t, 4.0f * ej.w * el.w);
+        const float S = s + v;
+        if (!(H > S * fmaf(g.ha, S, g.hb))) code = kCodeExact;
+      }
+      if (code == kCodeExact) {
+        ++c.n_exact_tri;
+        exact = true;
+        xe.ai = c.ai;
+        xe.pj = c.l2.P(j, a.ks);
+        xe.pl = c.l3.P(l, a.ks);
+        xe.meta = (mj >> 8) | ((ml >> 8) << 5) | ((mj & 0xffu) << 10) | ((ml & 0xffu) << 18);
+      } else if (code < static_cast<unsigned>(nb)) {
+        const float wprod = WEIGHTED ? (c.wa * c.l2.W(j, a.ks)) * c.l3.W(l, a.ks) * a.wscale : 0.0f;
+        hist_add<WEIGHTED, HG>(c.hist_s, a, (key_jl + code) * c.cs, wprod);
+      }
+    }
+    const unsigned xbal = __ballot_sync(0xffffffffu, exact);
+    if (c.xn + __popc(xbal) > 32) cold_flush_exact<SURVEY, WEIGHTED>(c);
+    if (exact) c.xbuf[c.xn + __popc(xbal & c.lt_mask)] = xe;
+    c.xn += __popc(xbal);
+    __syncwarp();
+  }
+  c.qn = 0;
+  __syncwarp();
+}
+
+// Re-examines row j of a work item (lane's l-entries el[r] at lb + 32r + lane)
+// and queues the candidates that need the careful/exact path, with the same
+// decisions the counting body took. Inline: it only recomputes flags.
+template <bool WEIGHTED, bool HG, bool DIAG>
+__device__ __forceinline__ void enqueue_row(Cold& c, const Geom& g, int j, float4 ej, const float4 (&el)[kReg],
+                                            int lb, int rmin, unsigned tab_adj, unsigned tab_last,
+                                            unsigned nb_cs) {
+  const float a4 = 4.0f * ej.w;
+  ++c.n_flag_rows;
+#pragma unroll
+  for (int r = 0; r < kReg; ++r) {
+    const int lr = lb + r * 32 + static_cast<int>(c.lane);
+    bool want = false;
+    if (!DIAG || r >= rmin) {
+      if (!WEIGHTED && !HG) {
+        want = cand_flag(ej.x, ej.y, ej.z, ej.w, a4, el[r].x, el[r].y, el[r].z, el[r].w,
+                         DIAG ? static_cast<unsigned>(j < lr) : 1u, g.tab_scale, tab_adj, tab_last, nb_cs, g.ha,
+                         g.hb) != 0;
+      } else {
+        const float dx = ej.x - el[r].x;
+        const float dy = ej.y - el[r].y;
+        const float dz = ej.z - el[r].z;
+        const float v = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+        const unsigned code = table_code(v, c.tab, g.tab_scale, g.tab_n);
+        const float b = el[r].w;
+        const float s = ej.w + b;
+        const float t = v - s;
+        const float H = fmaf(-t, t, a4 * b);
+        const float S = s + v;
+        const bool clean = H > S * fmaf(g.ha, S, g.hb);
+        want = code == kCodeCareful || (code < nb_cs && !clean);
+        if (DIAG) want = want && (j < lr);
+      }
+    }
+    const unsigned bal = __ballot_sync(0xffffffffu, want);
+    if (want)
+      c.queue[c.qn + __popc(bal & c.lt_mask)] =
+          static_cast<unsigned long long>(j) | (static_cast<unsigned long long>(lr) << 32);
+    c.qn += __popc(bal);
+    if (c.lane == 0) c.n_queued += __popc(bal);
+  }
+  __syncwarp();
+}
+
+// Exact r1^2 of a pair-stage candidate and its bin (or kCodeReject).
+static __device__ __noinline__ unsigned cold_pair_exact(const Geom* g, const double* sqr_bins, double4_16a pa,
+                                                        double px, double py, double pz) {
+  const double r = sqr_sep_exact(pa.x, pa.y, pa.z, px, py, pz, g->fma_pattern);
+  return (r < g->sqr_rmax && r > g->sqr_rmin) ? static_cast<unsigned>(exact_bin(r, sqr_bins, g->nb)) : kCodeReject;
 }
 
 template <bool SURVEY, bool SYM, bool WEIGHTED, bool HG>
@@ -212,7 +538,6 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
   const SmemLayout L = make_layout(nb, a.ks, SYM, WEIGHTED, HG);
   unsigned char* tab = smem + L.table;
   unsigned char* hist_s = smem + L.hist;
-  unsigned long long* queue = reinterpret_cast<unsigned long long*>(smem + L.queue) + warp * kQueueCap;
   const int nbin = nb * nb * nb;
   const int cs = a.code_scale;
   const unsigned nb_cs = static_cast<unsigned>(nb * cs);
@@ -256,7 +581,30 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
   }
   if (tid == 0) s_since = 0;
 
-  unsigned long long n_exact_tri = 0, n_exact_pair = 0, n_anchor = 0, n_pairs = 0, n_evals = 0;
+  Cold c;
+  c.a = a.self;
+  c.l2 = l2;
+  c.l3 = l3;
+  c.queue = reinterpret_cast<unsigned long long*>(smem + L.queue) + warp * kQueueCap;
+  c.xbuf = reinterpret_cast<ExactEntry*>(smem + L.xbuf) + warp * 32;
+  c.e2lo = s_e2lo;
+  c.e2hi = s_e2hi;
+  c.sqr_bins = s_sqr_bins;
+  c.tab = tab;
+  c.hist_s = hist_s;
+  c.qn = 0;
+  c.xn = 0;
+  c.nb = nb;
+  c.cs = cs;
+  c.ai = 0;
+  c.wa = 0.0f;
+  c.lane = static_cast<unsigned>(lane);
+  c.lt_mask = lt_mask;
+  c.n_exact_tri = 0;
+  c.n_queued = 0;
+  c.n_flag_rows = 0;
+
+  unsigned long long n_exact_pair = 0, n_anchor = 0, n_pairs = 0, n_evals = 0;
 
   auto flush = [&]() {
     for (int i = tid; i < (HG ? 0 : nbin); i += kThreads) {
@@ -278,6 +626,14 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
     }
   };
 
+  // Addresses in the shared window, for the PTX candidate body.
+  const unsigned tab_sh = static_cast<unsigned>(__cvta_generic_to_shared(tab));
+  const unsigned tab_adj = tab_sh - 0x4B000000u;
+  const unsigned tab_last = tab_sh + static_cast<unsigned>(g.tab_n - 1);
+  const unsigned hist_sh = static_cast<unsigned>(__cvta_generic_to_shared(hist_s));
+  const unsigned dummy = static_cast<unsigned>(__cvta_generic_to_shared(smem + L.scratch)) + 4u * lane;
+  const float tscale = g.tab_scale, ha = g.ha, hb = g.hb;
+
   for (;;) {
     __syncthreads();
     if (tid == 0) s_anchor = atomicAdd(a.work, 1);
@@ -295,28 +651,28 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
     // ---- slots: 27 (cell, image) pairs, order of source/cudaNcorr.cu:37-48
     if (tid < 27) {
       const int s = tid;
-      int c[3] = {hx + s / 9 - 1, hy + (s / 3) % 3 - 1, hz + s % 3 - 1};
+      int cc[3] = {hx + s / 9 - 1, hy + (s / 3) % 3 - 1, hz + s % 3 - 1};
       const int h[3] = {hx, hy, hz};
       double sh[3] = {0.0, 0.0, 0.0};
       bool ok = true;
       for (int d = 0; d < 3; ++d) {
         if (SURVEY) {
-          if (c[d] == g.nc[d] || c[d] == -1) ok = false;
+          if (cc[d] == g.nc[d] || cc[d] == -1) ok = false;
         } else {
-          if (c[d] == g.nc[d]) {
-            c[d] = 0;
+          if (cc[d] == g.nc[d]) {
+            cc[d] = 0;
             sh[d] = g.box[d];
-          } else if (c[d] == -1) {
-            c[d] = g.nc[d] - 1;
+          } else if (cc[d] == -1) {
+            cc[d] = g.nc[d] - 1;
             sh[d] = -g.box[d];
           }
         }
       }
-      const int cell = ok ? c[2] + g.nc[2] * (c[1] + g.nc[1] * c[0]) : -1;
+      const int cell = ok ? cc[2] + g.nc[2] * (cc[1] + g.nc[1] * cc[0]) : -1;
       for (int d = 0; d < 3; ++d) {
         s_shift[s][d] = sh[d];
         if (ok) {
-          const double o_n = __dmul_rn(static_cast<double>(c[d]), g.cell);
+          const double o_n = __dmul_rn(static_cast<double>(cc[d]), g.cell);
           const double o_h = __dmul_rn(static_cast<double>(h[d]), g.cell);
           s_do[s][d] = __double2float_rn(__dsub_rn(__dadd_rn(o_n, sh[d]), o_h));
         } else {
@@ -368,10 +724,12 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
           if (vp < g.pre_hi && vp > g.pre_lo && (!after_only || j > ai)) {
             // Exact anchor-relative offset of the image (FP64), rounded once.
             const double4_16a p = cat.pd[j];
-            const double Dx = __dsub_rn(__dadd_rn(p.x, s_shift[s][0]), pa.x);
-            const double Dy = __dsub_rn(__dadd_rn(p.y, s_shift[s][1]), pa.y);
-            const double Dz = __dsub_rn(__dadd_rn(p.z, s_shift[s][2]), pa.z);
-            const float dx = __double2float_rn(Dx), dy = __double2float_rn(Dy), dz = __double2float_rn(Dz);
+            const double px = __dadd_rn(p.x, s_shift[s][0]);
+            const double py = __dadd_rn(p.y, s_shift[s][1]);
+            const double pz = __dadd_rn(p.z, s_shift[s][2]);
+            const float dx = __double2float_rn(__dsub_rn(px, pa.x));
+            const float dy = __double2float_rn(__dsub_rn(py, pa.y));
+            const float dz = __double2float_rn(__dsub_rn(pz, pa.z));
             const float v = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
             unsigned code = table_code(v, tab, g.tab_scale, g.tab_n);
             if (code < nb_cs) {
@@ -381,11 +739,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
             }
             if (code == kCodeExact) {
               ++n_exact_pair;
-              const double r = sqr_sep_exact(pa.x, pa.y, pa.z, __dadd_rn(p.x, s_shift[s][0]),
-                                             __dadd_rn(p.y, s_shift[s][1]), __dadd_rn(p.z, s_shift[s][2]),
-                                             g.fma_pattern);
-              code = (r < g.sqr_rmax && r > g.sqr_rmin) ? static_cast<unsigned>(exact_bin(r, s_sqr_bins, nb))
-                                                        : kCodeReject;
+              code = cold_pair_exact(&a.self->g, s_sqr_bins, pa, px, py, pz);
             }
             if (code < static_cast<unsigned>(nb)) {
               acc = true;
@@ -443,6 +797,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
     // (weighted mode, |term| <= 2^30).
     const long long kItemLimit = (1LL << 31) / (static_cast<long long>(kSubJ) * kTile);
     const float wa = static_cast<float>(pa.w);
+    c.ai = ai;
+    c.wa = wa;
 
     for (long long m0 = 0; m0 < nitems; m0 += kItemLimit) {
       const long long m1 = min(nitems, m0 + kItemLimit);
@@ -457,57 +813,6 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
         s_item = 0;
       }
       __syncthreads();
-
-      int qn = 0;  // warp-uniform queue fill
-      // Settles queued candidates, 32 per round.
-      auto drain = [&]() {
-        for (int q0 = 0; q0 < qn; q0 += 32) {
-          const int qi = q0 + lane;
-          if (qi < qn) {
-            const unsigned long long pr = queue[qi];
-            const int j = static_cast<int>(pr & 0xffffffffu);
-            const int l = static_cast<int>(pr >> 32);
-            const float4 ej = l2.E(j, a.ks);
-            const unsigned mj = l2.M(j, a.ks);
-            const float4 el = l3.E(l, a.ks);
-            const unsigned ml = l3.M(l, a.ks);
-            const float dx = ej.x - el.x, dy = ej.y - el.y, dz = ej.z - el.z;
-            const float v = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-            const unsigned key_jl = ((mj & 0xffu) * nb * nb + (ml & 0xffu) * nb);
-            unsigned code = careful_code(v, s_e2lo, s_e2hi, nb, g.ka, g.kb);
-            if (code < static_cast<unsigned>(nb)) {
-              const float s = ej.w + el.w, t = v - s;
-              const float H = fmaf(-t, t, 4.0f * ej.w * el.w);
-              const float S = s + v;
-              if (!(H > S * fmaf(g.ha, S, g.hb))) code = kCodeExact;
-            }
-            if (code == kCodeExact) {
-              ++n_exact_tri;
-              const int pj = l2.P(j, a.ks);
-              const int pl = l3.P(l, a.ks);
-              const int sj = static_cast<int>(mj >> 8), sl = static_cast<int>(ml >> 8);
-              const double4_16a dj = a.c2.pd[pj];
-              const double4_16a dl = a.c3.pd[pl];
-              const double jx = __dadd_rn(dj.x, s_shift[sj][0]), jy = __dadd_rn(dj.y, s_shift[sj][1]),
-                           jz = __dadd_rn(dj.z, s_shift[sj][2]);
-              const double lx = __dadd_rn(dl.x, s_shift[sl][0]), ly = __dadd_rn(dl.y, s_shift[sl][1]),
-                           lz = __dadd_rn(dl.z, s_shift[sl][2]);
-              const double r1 = sqr_sep_exact(pa.x, pa.y, pa.z, jx, jy, jz, g.fma_pattern);
-              const double r2 = sqr_sep_exact(pa.x, pa.y, pa.z, lx, ly, lz, g.fma_pattern);
-              const double r3 = sqr_sep_exact(jx, jy, jz, lx, ly, lz, g.fma_pattern);
-              code = kCodeReject;
-              if (r3 < g.sqr_rmax && r3 > g.sqr_rmin && exact_triangle_ok(r1, r2, r3))
-                code = static_cast<unsigned>(exact_bin(r3, s_sqr_bins, nb));
-            }
-            if (code < static_cast<unsigned>(nb)) {
-              const float wprod = WEIGHTED ? (wa * l2.W(j, a.ks)) * l3.W(l, a.ks) * a.wscale : 0.0f;
-              hist_add<WEIGHTED, HG>(hist_s, a, (key_jl + code) * cs, wprod);
-            }
-          }
-        }
-        qn = 0;
-        __syncwarp();
-      };
 
       // One work item: l-tile lt (registers) against 32 j-entries of tile jt.
       auto item = [&](int jt, int lt, int sub, auto diag_tag) {
@@ -538,109 +843,108 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
         const unsigned* mj_base = j_in_smem ? l2.m + jb : l2.sm + (jb - a.ks);
         const float* wj_base = WEIGHTED ? (j_in_smem ? l2.w + jb : l2.sw + (jb - a.ks)) : nullptr;
         const unsigned kj_mul = static_cast<unsigned>(nb * nb * cs);
-        // Shared-window addresses: table entry = tab_adj + bits(y), clamped;
-        // histogram byte address = hist_sh + kj + kl + code.
-        const unsigned tab_sh = static_cast<unsigned>(__cvta_generic_to_shared(tab));
-        const unsigned tab_adj = tab_sh - 0x4B000000u;
-        const unsigned tab_last = tab_sh + static_cast<unsigned>(g.tab_n - 1);
-        const unsigned hist_sh = static_cast<unsigned>(__cvta_generic_to_shared(hist_s));
-        const float tscale = g.tab_scale, ha = g.ha, hb = g.hb;
+        const int rmin = DIAG ? sub : 0;  // l-slices r < sub lie entirely below these rows
+        // Rows with a candidate needing the careful/exact path are flagged
+        // here and re-examined out of line after the loop.
+        unsigned rowmask = 0;
 
-        // One j-entry against the lane's kReg l-entries; returns true when a
-        // candidate needs the careful/exact path.
-        auto jrow = [&](int j) -> bool {
-          const float4 ej = ej_base[j - jb];
-          const unsigned kj = (mj_base[j - jb] & 0xffu) * kj_mul + (HG ? 0u : hist_sh);
-          const float a4 = 4.0f * ej.w;
-          const float wja = WEIGHTED ? wa * wj_base[j - jb] * a.wscale : 0.0f;
-          bool q = false;
-#pragma unroll
-          for (int r = 0; r < kReg; ++r) {
-            const float dx = ej.x - el[r].x;
-            const float dy = ej.y - el[r].y;
-            const float dz = ej.z - el[r].z;
-            const float v = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-            const float y = fmaf(v, tscale, 8388608.0f);
-            const unsigned code = lds_u8(min(__float_as_uint(y) + tab_adj, tab_last));
-            const float b = el[r].w;
-            const float s = ej.w + b;
-            const float t = v - s;
-            const float H = fmaf(-t, t, a4 * b);
-            const float S = s + v;
-            const bool clean = H > S * fmaf(ha, S, hb);
-            bool ok = code < nb_cs;
-            bool careful = code == kCodeCareful;
-            if (DIAG) {
-              const bool in = j < lb + r * 32 + lane;
-              ok = ok && in;
-              careful = careful && in;
+        if (!WEIGHTED && !HG) {
+          // Unweighted, shared histogram: the PTX candidate body. The lane's
+          // four l-entries are explicit scalars; slices below the diagonal
+          // are skipped with a warp-uniform test.
+          const float4 L0 = el[0], L1 = el[1], L2 = el[2], L3 = el[3];
+          const unsigned K0 = kl[0], K1 = kl[1], K2 = kl[2], K3 = kl[3];
+          const int lr0 = lb + lane, lr1 = lr0 + 32, lr2 = lr0 + 64, lr3 = lr0 + 96;
+          auto row = [&](float4 e, unsigned k, int jj) -> unsigned {
+            const float a4 = 4.0f * e.w;
+            unsigned q = 0;
+            if (!DIAG || rmin <= 0)
+              q |= cand_count<DIAG>(e.x, e.y, e.z, e.w, a4, L0.x, L0.y, L0.z, L0.w, k, K0, jj < lr0, tscale,
+                                    tab_adj, tab_last, nb_cs, ha, hb, dummy);
+            if (!DIAG || rmin <= 1)
+              q |= cand_count<DIAG>(e.x, e.y, e.z, e.w, a4, L1.x, L1.y, L1.z, L1.w, k, K1, jj < lr1, tscale,
+                                    tab_adj, tab_last, nb_cs, ha, hb, dummy);
+            if (!DIAG || rmin <= 2)
+              q |= cand_count<DIAG>(e.x, e.y, e.z, e.w, a4, L2.x, L2.y, L2.z, L2.w, k, K2, jj < lr2, tscale,
+                                    tab_adj, tab_last, nb_cs, ha, hb, dummy);
+            q |= cand_count<DIAG>(e.x, e.y, e.z, e.w, a4, L3.x, L3.y, L3.z, L3.w, k, K3, jj < lr3, tscale,
+                                  tab_adj, tab_last, nb_cs, ha, hb, dummy);
+            return __any_sync(FULL, q != 0) ? 1u : 0u;
+          };
+          int j = jb;
+          if (j_in_smem) {
+            const unsigned e_sh = static_cast<unsigned>(__cvta_generic_to_shared(l2.e + jb));
+            const unsigned m_sh = static_cast<unsigned>(__cvta_generic_to_shared(l2.m + jb));
+#if NCORR_ROW_UNROLL == 2
+            for (; j + 1 < je; j += 2) {
+              const unsigned o = static_cast<unsigned>(j - jb);
+              const float4 e0 = lds_f4(e_sh + 16u * o);
+              const float4 e1 = lds_f4(e_sh + 16u * o + 16u);
+              const unsigned k0 = (lds_u32(m_sh + 4u * o) & 0xffu) * kj_mul + hist_sh;
+              const unsigned k1 = (lds_u32(m_sh + 4u * o + 4u) & 0xffu) * kj_mul + hist_sh;
+              const unsigned f0 = row(e0, k0, j);
+              const unsigned f1 = row(e1, k1, j + 1);
+              rowmask |= (f0 | (f1 << 1)) << o;
             }
-            const unsigned key = kj + kl[r] + code;
-            if (HG) {
-              if (ok && clean) hist_add<WEIGHTED, true>(hist_s, a, key, wja * wl[r]);
-            } else if (WEIGHTED) {
-              red_shared_u64_if(key, static_cast<unsigned long long>(__float2ll_rn(wja * wl[r])), ok && clean);
-            } else {
-              red_shared_u32_if(key, ok && clean);
+#endif
+            for (; j < je; ++j) {
+              const unsigned o = static_cast<unsigned>(j - jb);
+              const float4 e0 = lds_f4(e_sh + 16u * o);
+              const unsigned k0 = (lds_u32(m_sh + 4u * o) & 0xffu) * kj_mul + hist_sh;
+              rowmask |= row(e0, k0, j) << o;
             }
-            q = q || careful || (ok && !clean);
+          } else {
+            for (; j < je; ++j) {
+              const unsigned o = static_cast<unsigned>(j - jb);
+              rowmask |= row(ej_base[o], (mj_base[o] & 0xffu) * kj_mul + hist_sh, j) << o;
+            }
           }
-          return q;
-        };
-
-        // Queues the candidates of row j that need the careful/exact path.
-        auto enqueue_row = [&](int j) {
-          const float4 ej = ej_base[j - jb];
-          const float a4 = 4.0f * ej.w;
+        } else {
+          // Weighted sums or global histogram: the same decisions in C++.
+          for (int j = jb; j < je; ++j) {
+            const unsigned o = static_cast<unsigned>(j - jb);
+            const float4 ej = ej_base[o];
+            const unsigned kj = (mj_base[o] & 0xffu) * kj_mul + (HG ? 0u : hist_sh);
+            const float a4 = 4.0f * ej.w;
+            const float wja = WEIGHTED ? wa * wj_base[o] * a.wscale : 0.0f;
+            bool q = false;
 #pragma unroll
-          for (int r = 0; r < kReg; ++r) {
-            const float dx = ej.x - el[r].x;
-            const float dy = ej.y - el[r].y;
-            const float dz = ej.z - el[r].z;
-            const float v = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-            const unsigned code = table_code(v, tab, g.tab_scale, g.tab_n);
-            const float b = el[r].w;
-            const float s = ej.w + b;
-            const float t = v - s;
-            const float H = fmaf(-t, t, a4 * b);
-            const float S = s + v;
-            const bool clean = H > S * fmaf(g.ha, S, g.hb);
-            bool want = code == kCodeCareful || (code < nb_cs && !clean);
-            if (DIAG) want = want && (j < lb + r * 32 + lane);
-            const unsigned bal = __ballot_sync(FULL, want);
-            if (want) {
-              queue[qn + __popc(bal & lt_mask)] =
-                  static_cast<unsigned long long>(j) |
-                  (static_cast<unsigned long long>(lb + r * 32 + lane) << 32);
+            for (int r = 0; r < kReg; ++r) {
+              if (DIAG && r < rmin) continue;
+              const float dx = ej.x - el[r].x;
+              const float dy = ej.y - el[r].y;
+              const float dz = ej.z - el[r].z;
+              const float v = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+              const unsigned code = table_code(v, tab, g.tab_scale, g.tab_n);
+              const float b = el[r].w;
+              const float s = ej.w + b;
+              const float t = v - s;
+              const float H = fmaf(-t, t, a4 * b);
+              const float S = s + v;
+              const bool clean = H > S * fmaf(ha, S, hb);
+              bool ok = code < nb_cs;
+              bool careful = code == kCodeCareful;
+              if (DIAG) {
+                const bool in = j < lb + r * 32 + lane;
+                ok = ok && in;
+                careful = careful && in;
+              }
+              const unsigned key = kj + kl[r] + code;
+              if (HG) {
+                if (ok && clean) hist_add<WEIGHTED, true>(hist_s, a, key, wja * wl[r]);
+              } else {
+                red_shared_u64_if(key, static_cast<unsigned long long>(__float2ll_rn(wja * wl[r])), ok && clean);
+              }
+              q = q || careful || (ok && !clean);
             }
-            qn += __popc(bal);
-          }
-        };
-
-        int j = jb;
-        for (; j + 1 < je; j += 2) {
-          const bool q0 = jrow(j);
-          const bool q1 = jrow(j + 1);
-          const unsigned qm = __ballot_sync(FULL, q0) | (__ballot_sync(FULL, q1) ? 2u : 0u);
-          if (qm) {
-            if (qm & 1u) {
-              enqueue_row(j);
-              __syncwarp();
-              if (qn > kQueueCap - kTile) drain();
-            }
-            if (qm & 2u) {
-              enqueue_row(j + 1);
-              __syncwarp();
-              if (qn > kQueueCap - kTile) drain();
-            }
+            rowmask |= (__any_sync(FULL, q) ? 1u : 0u) << o;
           }
         }
-        if (j < je) {
-          if (__any_sync(FULL, jrow(j))) {
-            enqueue_row(j);
-            __syncwarp();
-            if (qn > kQueueCap - kTile) drain();
-          }
+        while (rowmask) {
+          const int bit = __ffs(rowmask) - 1;
+          rowmask &= rowmask - 1u;
+          if (c.qn > kQueueCap - kTile) cold_drain<SURVEY, WEIGHTED, HG>(c);
+          enqueue_row<WEIGHTED, HG, DIAG>(c, g, jb + bit, ej_base[bit], el, lb, rmin, tab_adj, tab_last, nb_cs);
         }
       };
 
@@ -668,20 +972,25 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
         else
           item(jt, lt, sub, std::false_type());
       }
-      __syncwarp();
-      drain();
+      // Queue entries refer to this anchor's lists: settle them now.
+      if (c.qn > 0) cold_drain<SURVEY, WEIGHTED, HG>(c);
       __syncthreads();
     }
   }
+  cold_flush_exact<SURVEY, WEIGHTED>(c);
   __syncthreads();
   flush();
   if (a.stats) {
-    atomicAdd(&a.stats[0], n_exact_tri);
+    atomicAdd(&a.stats[0], c.n_exact_tri);
     atomicAdd(&a.stats[1], n_exact_pair);
     if (tid == 0) {
       atomicAdd(&a.stats[2], n_anchor);
       atomicAdd(&a.stats[3], n_pairs);
       atomicAdd(&a.stats[4], n_evals);
+    }
+    if (lane == 0) {
+      atomicAdd(&a.stats[5], c.n_flag_rows);
+      atomicAdd(&a.stats[6], c.n_queued);
     }
   }
 }

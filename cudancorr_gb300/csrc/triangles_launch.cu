@@ -62,6 +62,23 @@ int triangles_occupancy(bool survey, bool sym, bool weighted, bool hg, size_t sm
   return weighted ? occupancy_hg<false, false, true>(hg, smem) : occupancy_hg<false, false, false>(hg, smem);
 }
 
+template <bool SURVEY, bool WEIGHTED>
+__global__ void __launch_bounds__(256) k_exact(KArgs a) {
+  const unsigned n = min(*a.xq_count, a.xq_cap);
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    settle_exact<SURVEY, WEIGHTED>(a, a.xq[i]);
+}
+
+void launch_exact(const KArgs& a, bool survey, bool weighted, int grid, cudaStream_t st) {
+  if (survey) {
+    if (weighted) k_exact<true, true><<<grid, 256, 0, st>>>(a);
+    else k_exact<true, false><<<grid, 256, 0, st>>>(a);
+  } else {
+    if (weighted) k_exact<false, true><<<grid, 256, 0, st>>>(a);
+    else k_exact<false, false><<<grid, 256, 0, st>>>(a);
+  }
+}
+
 // Folds the unsorted (bin_j, bin_l, bin_3) histogram into the reference's
 // triCountsAll_ layout: out[hi + mid*nb + lo*nb^2] for lo <= mid <= hi sums
 // the distinct permutations in a fixed order (deterministic), times `factor`

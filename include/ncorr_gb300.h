@@ -56,6 +56,8 @@ typedef struct ncorr_stats {
   uint64_t n_exact_pairs;  /* neighbours settled by the FP64 path */
   uint64_t n_exact_tris;   /* triangles settled by the FP64 path */
   uint64_t triangles;      /* sum of the full histogram (count mode) */
+  uint64_t n_flagged_rows; /* neighbour rows re-examined for uncertain candidates */
+  uint64_t n_queued;       /* candidates settled by the careful band or the FP64 path */
   int weighted;            /* 1: some weight != 1.0 (fixed-point weighted sums) */
   int symmetric;           /* orderings each visited triangle stands for: 1 (all (j,l)),
                               2 (p2 == p3: pairs j<l), 6 (p1 == p2 == p3 in a geometry

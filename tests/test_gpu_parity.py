@@ -164,6 +164,21 @@ def test_box_face_point_is_clamped(engine_lib, oracle):
     assert np.array_equal(h, ref) and ref.sum() > 0
 
 
+def test_exact_queue_overflow_settles_in_place(engine_lib, oracle, monkeypatch):
+    """With no room in the deferred exact queue every uncertain candidate is
+    settled inside the triangle kernel; results are unchanged."""
+    c = cases.fma_probe()
+    monkeypatch.setenv("NCORR_EXACT_QUEUE_CAP", "0")
+    h0, _, st0 = run_engine(c["box"], c["edges"], c["p"])
+    monkeypatch.setenv("NCORR_EXACT_QUEUE_CAP", "3")
+    h3, _, _ = run_engine(c["box"], c["edges"], c["p"])
+    monkeypatch.delenv("NCORR_EXACT_QUEUE_CAP")
+    h, _, _ = run_engine(c["box"], c["edges"], c["p"])
+    ref = oracle.count_threeD(c["box"], c["edges"], c["p"])
+    assert np.array_equal(h0, ref) and np.array_equal(h3, ref) and np.array_equal(h, ref)
+    assert st0["n_exact_tris"] + st0["n_exact_pairs"] > 0
+
+
 def test_repeatable(engine_lib):
     p, box, edges = cases.small_box_clustered()
     h1, _, _ = run_engine(box, edges, p)
