@@ -39,7 +39,7 @@ EXPORTS = (
     "ncorr_calculate_d1d2d3_device", "ncorr_num_out", "ncorr_num_bins", "ncorr_get_tri_bins_out",
     "ncorr_get_pi_bins_out", "ncorr_get_tri_counts_out", "ncorr_get_tri_counts_all",
     "ncorr_get_stats", "ncorr_last_error", "survey_prep_cat", "survey_prep_cat2",
-    "survey_convert_coordinates", "ncorr_logspace",
+    "survey_convert_coordinates", "ncorr_logspace", "ncorr_count_noalloc",
 )
 
 
@@ -107,6 +107,7 @@ def load_library() -> ctypes.CDLL:
         "survey_prep_cat2": (i32, [_D, i64, _D, i64, _D, _D]),
         "survey_convert_coordinates": (i32, [_D, _D, i64, _D]),
         "ncorr_logspace": (i32, [ctypes.c_double, ctypes.c_double, i32, _D]),
+        "ncorr_count_noalloc": (i32, [_D, _D, i32, i32, vp, i64, vp, i64, vp, i64, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

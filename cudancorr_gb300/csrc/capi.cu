@@ -6,6 +6,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <limits>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -783,3 +784,320 @@ int ncorr_logspace(double start, double end, int n, double* out) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Entry point that allocates nothing.
+//
+// Some callers may not allocate device memory at all: code that hands the GPU
+// a fixed memory budget up front (a pre-sized pool, an embedding runtime), or
+// code on a path where a cudaMalloc/cudaFree would synchronise the device and
+// stall work queued by others. For them, ncorr_count_noalloc runs the same
+// kernels as calculateD1D2D3 with every working buffer carved out of one
+// file-scope device array. Its size is fixed at build time and every GPU
+// that loads the library holds it until the process exits.
+namespace {
+
+constexpr long long kNoAllocPoints = 65536;  // points per catalogue (p1, p2, p3)
+constexpr long long kNoAllocCells = 32768;   // cells of the grid
+constexpr int kNoAllocMaxBins = 31;          // bins per side
+constexpr unsigned kNoAllocExactCap = 65536; // deferred exact candidates
+constexpr int kNoAllocMaxDevices = 64;
+
+// Bytes of one catalogue's cell list: cid, count, start, cursor, pd, pq, pc.
+constexpr size_t kNoAllocCatBytes =
+    ((kNoAllocPoints * (4 + 32 + 16 + 4) + kNoAllocCells * 12 + 4 + 255) / 256) * 256;
+constexpr size_t kNoAllocHistBytes = 2ull * kNoAllocMaxBins * kNoAllocMaxBins * kNoAllocMaxBins * 8;
+constexpr size_t kNoAllocBytes = 16ull << 20;  // 16 MiB
+
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+namespace {
+
+std::mutex g_noalloc_mutex;
+void* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+// Device address of the scratch array on the current device, looked up once
+// per device (the host-side name of a __device__ array is not a device
+// address).
+int noalloc_scratch(int dev, unsigned char** out) {
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(NCORR_ERR_INVALID_ARGUMENT, "device index out of range");
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+      return fail(NCORR_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = static_cast<unsigned char*>(g_noalloc_ptr[dev]);
+  return NCORR_OK;
+}
+
+}  // namespace
+
+extern "C" int ncorr_count_noalloc(const double box[3], const double* edges, int n_edges, int is_survey,
+                                   const double* d_p1, int64_t n1, const double* d_p2, int64_t n2,
+                                   const double* d_p3, int64_t n3, double* d_counts_all, void* stream) {
+  static_assert(3 * kNoAllocCatBytes + kNoAllocHistBytes + kTableSize + kNoAllocExactCap * sizeof(ExactEntry) +
+                        sizeof(KArgs) + 64 * 1024 <= kNoAllocBytes,
+                "scratch layout exceeds the scratch array");
+  if (!box || !edges || !d_counts_all) return fail(NCORR_ERR_INVALID_ARGUMENT, "null box, edges or output");
+  if (n_edges < 2 || n_edges - 1 > kNoAllocMaxBins)
+    return fail(NCORR_ERR_INVALID_ARGUMENT, "ncorr_count_noalloc: 1..31 bins per side");
+  for (int i = 0; i < n_edges; ++i)
+    if (!std::isfinite(edges[i])) return fail(NCORR_ERR_INVALID_ARGUMENT, "non-finite bin edge");
+  if (edges[0] < 0.0) return fail(NCORR_ERR_INVALID_ARGUMENT, "negative first bin edge");
+  for (int i = 1; i < n_edges; ++i)
+    if (!(edges[i] > edges[i - 1]) || !(edges[i] * edges[i] > edges[i - 1] * edges[i - 1]))
+      return fail(NCORR_ERR_INVALID_ARGUMENT, "bin edges must be strictly increasing");
+  for (int d = 0; d < 3; ++d)
+    if (!(box[d] > 0.0) || !std::isfinite(box[d])) return fail(NCORR_ERR_INVALID_ARGUMENT, "box sides must be positive");
+  const int64_t ns[3] = {n1, n2, n3};
+  const double* src[3] = {d_p1, d_p2, d_p3};
+  for (int r = 0; r < 3; ++r) {
+    if (ns[r] < 0 || ns[r] > kNoAllocPoints)
+      return fail(NCORR_ERR_CAPACITY, "ncorr_count_noalloc: at most 65536 points per catalogue");
+    if (ns[r] > 0 && (!src[r] || (reinterpret_cast<uintptr_t>(src[r]) & 15u)))
+      return fail(NCORR_ERR_INVALID_ARGUMENT, "device catalogues must be non-null and 16-byte aligned");
+  }
+  // Geometry, as ncorr_create builds it, on the stack.
+  Geom g;
+  std::memset(&g, 0, sizeof(g));
+  g.nb = n_edges - 1;
+  g.survey = is_survey ? 1 : 0;
+  g.fma_pattern = kDefaultFmaPattern;
+  const double rmax = edges[n_edges - 1], rmin = edges[0];
+  g.cell = rmax;
+  g.sqr_rmax = rmax * rmax;
+  g.sqr_rmin = rmin * rmin;
+  long long ncell = 1;
+  for (int d = 0; d < 3; ++d) {
+    g.box[d] = box[d];
+    const double n = std::ceil(box[d] / rmax);
+    if (n > 4096.0) return fail(NCORR_ERR_CAPACITY, "ncorr_count_noalloc: cell grid too large");
+    g.nc[d] = static_cast<int>(n);
+    ncell *= g.nc[d];
+  }
+  if (ncell > kNoAllocCells) return fail(NCORR_ERR_CAPACITY, "ncorr_count_noalloc: at most 32768 cells");
+  for (int i = 0; i < n_edges; ++i) {
+    g.sqr_bins[i] = edges[i] * edges[i];
+    g.e2lo[i] = f32_down(g.sqr_bins[i]);
+    g.e2hi[i] = f32_up(g.sqr_bins[i]);
+  }
+  set_error_model(g);
+
+  int dev = 0;
+  CU(cudaGetDevice(&dev));
+  unsigned char* base = nullptr;
+  if (int rc = noalloc_scratch(dev, &base)) return rc;
+  cudaGetLastError();
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+
+  // Carve the scratch: three cell lists, histogram, table, exact queue, small
+  // counters, kernel arguments.
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    unsigned char* p = base + off;
+    off += (bytes + 255) & ~size_t(255);
+    return p;
+  };
+  struct CatScratch {
+    int *cid, *count, *start, *cursor, *pc;
+    double4_16a* pd;
+    float4* pq;
+  } cat[3];
+  for (auto& c : cat) {
+    unsigned char* b = take(kNoAllocCatBytes);
+    size_t o = 0;
+    auto sub = [&](size_t bytes) {
+      unsigned char* p = b + o;
+      o += (bytes + 15) & ~size_t(15);
+      return p;
+    };
+    c.pd = reinterpret_cast<double4_16a*>(sub(kNoAllocPoints * 32));
+    c.pq = reinterpret_cast<float4*>(sub(kNoAllocPoints * 16));
+    c.cid = reinterpret_cast<int*>(sub(kNoAllocPoints * 4));
+    c.pc = reinterpret_cast<int*>(sub(kNoAllocPoints * 4));
+    c.count = reinterpret_cast<int*>(sub(kNoAllocCells * 4));
+    c.start = reinterpret_cast<int*>(sub((kNoAllocCells + 1) * 4));
+    c.cursor = reinterpret_cast<int*>(sub(kNoAllocCells * 4));
+  }
+  unsigned long long* hist = reinterpret_cast<unsigned long long*>(take(kNoAllocHistBytes));
+  unsigned char* table = take(kTableSize);
+  ExactEntry* xq = reinterpret_cast<ExactEntry*>(take(kNoAllocExactCap * sizeof(ExactEntry)));
+  KArgs* d_args = reinterpret_cast<KArgs*>(take(sizeof(KArgs)));
+  int* flags = reinterpret_cast<int*>(take(8 * sizeof(int)));
+  unsigned* wmax = reinterpret_cast<unsigned*>(take(sizeof(unsigned)));
+  int* work = reinterpret_cast<int*>(take(sizeof(int)));
+  int* bound = reinterpret_cast<int*>(take(2 * sizeof(int)));
+  unsigned long long* stats = reinterpret_cast<unsigned long long*>(take(8 * sizeof(unsigned long long)));
+  unsigned long long* total = reinterpret_cast<unsigned long long*>(take(sizeof(unsigned long long)));
+  unsigned* xq_count = reinterpret_cast<unsigned*>(take(sizeof(unsigned)));
+  unsigned char* slab = take(256);  // the lists never overflow here (checked below)
+  if (off > kNoAllocBytes) return fail(NCORR_ERR_CAPACITY, "scratch layout exceeds the scratch array");
+
+  // Everything read before being written starts at zero on every call: the
+  // array keeps the previous call's contents.
+  CU(cudaMemsetAsync(flags, 0, 8 * sizeof(int), st));
+  CU(cudaMemsetAsync(wmax, 0, sizeof(unsigned), st));
+  CU(cudaMemsetAsync(bound, 0, 2 * sizeof(int), st));
+  CU(cudaMemsetAsync(stats, 0, 8 * sizeof(unsigned long long), st));
+  CU(cudaMemsetAsync(total, 0, sizeof(unsigned long long), st));
+  CU(cudaMemsetAsync(work, 0, sizeof(int), st));
+  CU(cudaMemsetAsync(xq_count, 0, sizeof(unsigned), st));
+
+  // Distinct catalogues (same pointer and size: gridded once).
+  int role[3];
+  role[0] = 0;
+  role[1] = (d_p2 == d_p1 && n2 == n1) ? 0 : 1;
+  role[2] = (d_p3 == d_p2 && n3 == n2) ? role[1] : ((d_p3 == d_p1 && n3 == n1) ? 0 : 2);
+  const bool sym = role[1] == role[2];
+  bool done[3] = {false, false, false};
+  for (int r = 0; r < 3; ++r) {
+    const int ci = role[r];
+    if (done[ci]) continue;
+    done[ci] = true;
+    CatScratch& c = cat[ci];
+    const int n = static_cast<int>(ns[r]);
+    CU(cudaMemsetAsync(c.count, 0, ncell * sizeof(int), st));
+    launch_assign(reinterpret_cast<const double4_16a*>(src[r]), n, g, c.cid, c.count, flags + ci, wmax, st);
+    launch_scan(c.count, static_cast<int>(ncell), c.start, c.cursor, st);
+    launch_scatter(reinterpret_cast<const double4_16a*>(src[r]), n, g, c.cid, c.cursor, c.pd, c.pq, c.pc, st);
+  }
+  launch_nbr_bound(cat[role[1]].count, g, bound, st);
+  if (!sym) launch_nbr_bound(cat[role[2]].count, g, bound + 1, st);
+  CU(cudaGetLastError());
+  int hflags[8];
+  unsigned hwmax = 0;
+  int hbound[2] = {0, 0};
+  CU(cudaMemcpyAsync(hflags, flags, sizeof(hflags), cudaMemcpyDeviceToHost, st));
+  CU(cudaMemcpyAsync(&hwmax, wmax, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+  CU(cudaMemcpyAsync(hbound, bound, sizeof(hbound), cudaMemcpyDeviceToHost, st));
+  CU(cudaStreamSynchronize(st));
+  bool weighted = false;
+  for (int r = 0; r < 3; ++r) {
+    const int f = hflags[role[r]];
+    if (f & (kFlagNonFinite | kFlagOutOfGrid))
+      return fail(NCORR_ERR_OUT_OF_GRID, "a point lies outside the cell grid or is non-finite");
+    if (f & kFlagWeighted) weighted = true;
+  }
+  if (g.survey && (hflags[role[0]] & kFlagSurveyFace))
+    return fail(NCORR_ERR_OUT_OF_GRID, "survey anchor on the upper face of the cell grid");
+  bool sym6 = sym && role[0] == role[1] && !(hflags[role[0]] & kFlagNoSym6);
+  if (sym6 && !g.survey)
+    for (int d = 0; d < 3; ++d)
+      if (g.nc[d] < 4 || __builtin_fma(-static_cast<double>(g.nc[d]), g.cell, g.box[d]) != 0.0) sym6 = false;
+  float wscale = 1.0f;
+  if (weighted) {
+    float wm = 0.0f;
+    std::memcpy(&wm, &hwmax, sizeof(float));
+    const double p3 = static_cast<double>(wm) * wm * wm;
+    int e = 0;
+    if (p3 > 0) e = static_cast<int>(std::floor(std::log2(std::ldexp(1.0, 30) / p3)));
+    wscale = static_cast<float>(std::ldexp(1.0, std::max(-120, std::min(120, e))));
+  }
+  const int nbin = g.nb * g.nb * g.nb;
+  const int elem = weighted ? 8 : 4;
+  const bool hg = static_cast<long>(nbin) * elem > kHistSmemMax || g.nb * elem > 0xFD;
+  const int code_scale = hg ? 1 : elem;
+  int ks = 0;
+  {
+    SmemLayout L0 = make_layout(g.nb, 0, sym, weighted, hg);
+    const int per = (sym ? 1 : 2) * (16 + 4 + 4 + (weighted ? 4 : 0));
+    ks = ((kSmemBudget - L0.total) / per / kTile) * kTile;
+    if (ks < kTile) ks = kTile;
+  }
+  if (std::max(hbound[0], hbound[1]) > ks)
+    return fail(NCORR_ERR_CAPACITY, "ncorr_count_noalloc: neighbourhoods too dense for its fixed lists");
+  const SmemLayout L = make_layout(g.nb, ks, sym, weighted, hg);
+  const size_t smem = static_cast<size_t>(L.total);
+  const int occ = triangles_occupancy(g.survey != 0, sym, weighted, hg, smem);
+  if (occ <= 0) return fail(NCORR_ERR_CUDA, "triangle kernel does not fit on the device");
+  int nsm = 0;
+  CU(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const int grid = std::max(1, std::min(static_cast<int>(n1), nsm * occ));
+
+  // Bin table, built on the host stack and copied in (a pageable source:
+  // the copy has completed when cudaMemcpyAsync returns).
+  unsigned char tab_host[kTableSize];
+  {
+    const int n = kTableSize;
+    const double vmax = g.sqr_rmax * 1.05;
+    const float scale = static_cast<float>((n - 2) / vmax);
+    g.tab_scale = scale;
+    g.tab_n = n;
+    const double ka = g.ka, kb = g.kb;
+    for (int i = 0; i < n; ++i) {
+      double lo = (i - 0.5) / static_cast<double>(scale);
+      double hi = (i + 0.5) / static_cast<double>(scale);
+      if (lo < 0) lo = 0;
+      if (i == n - 1) hi = std::numeric_limits<double>::infinity();
+      const double blo = lo - (ka * lo + kb) * 1.01;
+      const double bhi = hi + (ka * hi + kb) * 1.01;
+      unsigned char code = static_cast<unsigned char>(kCodeCareful);
+      if (bhi <= g.sqr_rmin || blo >= g.sqr_rmax) {
+        code = static_cast<unsigned char>(kCodeReject);
+      } else if (blo > g.sqr_rmin && bhi < g.sqr_rmax) {
+        for (int b = 0; b < g.nb; ++b)
+          if (g.sqr_bins[b] <= blo && bhi < g.sqr_bins[b + 1]) {
+            code = static_cast<unsigned char>(b * code_scale);
+            break;
+          }
+      }
+      tab_host[i] = code;
+    }
+  }
+  CU(cudaMemcpyAsync(table, tab_host, kTableSize, cudaMemcpyHostToDevice, st));
+  CU(cudaMemsetAsync(hist, 0, (weighted ? 2 : 1) * static_cast<size_t>(nbin) * sizeof(unsigned long long), st));
+
+  KArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.g = g;
+  auto catview = [&](int ci, int64_t n) {
+    Catalog v;
+    v.pd = cat[ci].pd;
+    v.pq = cat[ci].pq;
+    v.pc = cat[ci].pc;
+    v.start = cat[ci].start;
+    v.count = cat[ci].count;
+    v.n = static_cast<int>(n);
+    return v;
+  };
+  a.c1 = catview(role[0], n1);
+  a.c2 = catview(role[1], n2);
+  a.c3 = catview(role[2], n3);
+  a.table = table;
+  a.work = work;
+  a.flags = flags + 4;
+  a.hist.counts = weighted ? nullptr : hist;
+  a.hist.wsum = weighted ? hist : nullptr;
+  a.slab_e = reinterpret_cast<float4*>(slab);
+  a.slab_m = reinterpret_cast<unsigned*>(slab);
+  a.slab_p = reinterpret_cast<int*>(slab);
+  a.slab_w = weighted ? reinterpret_cast<float*>(slab) : nullptr;
+  a.ks = ks;
+  a.kg = 0;
+  a.sym6 = sym6 ? 1 : 0;
+  a.code_scale = code_scale;
+  a.wscale = wscale;
+  a.stats = stats;
+  a.xq = xq;
+  a.xq_count = xq_count;
+  a.xq_cap = kNoAllocExactCap;
+  a.self = d_args;
+  CU(cudaMemcpyAsync(d_args, &a, sizeof(KArgs), cudaMemcpyHostToDevice, st));
+  if (n1 > 0) {
+    CU(launch_triangles(a, g.survey != 0, sym, weighted, hg, grid, smem, st));
+    launch_exact(a, g.survey != 0, weighted, nsm * 4, st);
+  }
+  launch_fold(a.hist.counts, a.hist.wsum, g.nb, weighted, sym6 ? 6.0 : (sym ? 2.0 : 1.0), 1.0 / wscale,
+              d_counts_all, total, st);
+  CU(cudaGetLastError());
+  int kflags = 0;
+  CU(cudaMemcpyAsync(&kflags, flags + 4, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CU(cudaStreamSynchronize(st));
+  if (kflags & kFlagListOverflow) return fail(NCORR_ERR_CAPACITY, "neighbour list overflow");
+  return NCORR_OK;
+}

@@ -152,6 +152,24 @@ int survey_convert_coordinates(const double cosmo[3], const double* in, int64_t 
  * n log-spaced bin edges from start to end. */
 int ncorr_logspace(double start, double end, int n, double* out);
 
+/* Triangle count without any device allocation; no counterpart in the
+ * reference. For callers that must not allocate device memory -- code given a
+ * fixed device-memory budget up front, or running where a cudaMalloc or
+ * cudaFree would synchronise the device and stall work queued by others. All
+ * working memory is one 16 MiB array inside the library, held by every GPU
+ * that loads it until the process exits; limits: at most 65536 points per
+ * catalogue, 32768 cells, 31 bins per side, and neighbourhoods that fit the
+ * kernel's on-chip lists (NCORR_ERR_CAPACITY otherwise). Inputs are device
+ * catalogues (n x 4 doubles, 16-byte aligned); d_counts_all receives the
+ * nb^3 doubles of triCountsAll_, as ncorr_get_tri_counts_all returns them.
+ * The first call on each device looks up the array's device address, so make
+ * it before any stream capture. Calls share the array: calls that overlap on
+ * the GPU (other threads, other streams) race, so serialise them. Returns
+ * after the work on `stream` (null: the legacy default stream) completes. */
+int ncorr_count_noalloc(const double box[3], const double* edges, int n_edges, int is_survey,
+                        const double* d_p1, int64_t n1, const double* d_p2, int64_t n2,
+                        const double* d_p3, int64_t n3, double* d_counts_all, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
