@@ -46,10 +46,11 @@ N_SM = 152
 FP32_LANES_PER_SM = 128
 L2_FLUSH_BYTES = 256 << 20
 # Triangle-kernel DRAM traffic per launch (dram__bytes_read.sum +
-# dram__bytes_write.sum) from the ncu capture summarised in
-# profiles/triangles_box_clustered_2M.md, scaled to the full launch; None
-# until that capture exists.
-TRIANGLE_KERNEL_DRAM_BYTES = None
+# dram__bytes_write.sum): 27.37 MB measured with ncu on the 249,814-point
+# box_clustered_L1000 workload, scaled by the anchor count to the
+# 2,001,574-point box_clustered launch.
+TRIANGLE_KERNEL_DRAM_BYTES = {"box_clustered": int(27.37e6 * 2001574 / 249814),
+                              "box_clustered_L1000": int(27.37e6)}
 
 
 def workload(name: str, seed_offset: int):
@@ -57,6 +58,13 @@ def workload(name: str, seed_offset: int):
     if name == "box_clustered":
         p, box, edges = C.config_box_clustered(seed=2 + seed_offset)
         desc = ("Neyman-Scott box: 200,000 parents x Poisson(10), sigma 2, L=2000 Mpc/h, "
+                "r_max=100, 20 linear bins, unweighted")
+    elif name == "box_clustered_L1000":
+        # Same process and density as box_clustered in one eighth of the
+        # volume (250,000 points): the per-anchor work is the same, so this is
+        # the small case for full ncu captures of the triangle kernel.
+        p, box, edges = C.neyman_scott(25000, 10.0, 2.0, 1000.0, 12 + seed_offset), 1000.0, C.linear_edges(100.0, 20)
+        desc = ("Neyman-Scott box: 25,000 parents x Poisson(10), sigma 2, L=1000 Mpc/h, "
                 "r_max=100, 20 linear bins, unweighted")
     elif name == "box_uniform":
         p, box, edges = C.config_box_uniform(seed=1 + seed_offset)
@@ -263,7 +271,8 @@ def run_engine(args) -> dict:
                 "ms_per_step": e2e_total / args.steps},
         "roofline": {"bound": "fp32_issue", "achieved": achieved, "peak": peak_tflops,
                      "unit": "TFLOP/s", "frac": achieved / peak_tflops,
-                     "traffic": TRIANGLE_KERNEL_DRAM_BYTES,
+                     "traffic": (TRIANGLE_KERNEL_DRAM_BYTES.get(args.workload)
+                                 if args.anchor_slab is None else None),
                      "kernel": "k_triangles", "kernel_ms": statistics.mean(kernel_ms),
                      "work": "8 flops x (candidate triangles W + pair-stage evaluations P) per launch",
                      "W": int(st_last["n_pairs"]), "P": int(st_last["n_pair_evals"]),
@@ -280,8 +289,18 @@ def run_engine(args) -> dict:
 
 
 def run_reference(args) -> dict:
-    """The reference's own kernel (oracle/_ref cubin) on a random anchor
-    sample of the same workload, through its host flow."""
+    """The reference's own kernel (oracle/_ref cubin, compiled unmodified from
+    its source/device.cu) behind a restatement of its host flow, on a random
+    anchor sample of the same workload.
+
+    The reference runs one thread per anchor in 64-thread blocks, so its
+    throughput depends on how many blocks each SM holds. Measured on GB300
+    (2M-point clustered box): 7.7e7 triangles/s with 8192 anchors (about one
+    block per SM), 2.47e8 with 38,912 (4 blocks per SM), 2.52e8 with 155,648
+    (16 per SM). The default sample of 38,912 anchors (152 SMs x 4 x 64)
+    reaches that plateau. A step takes about 86 s, which the slowest anchor
+    thread sets. Warm-up steps load the module and run the small uniform box.
+    """
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return None
@@ -291,19 +310,24 @@ def run_reference(args) -> dict:
     except Exception as e:  # the cubin is built where the reference sources are mounted
         return {"impl": "reference", "unavailable": f"reference kernel not loadable: {e}"}
     p, box, edges, desc = workload(args.workload, 0)
+    from cudancorr_gb300 import catalogs as C
+    wp, wbox, wedges = C.config_box_uniform()
+    for _ in range(args.warmup):
+        O.reference_count(wbox, wedges, wp[:4096], wp, wp)
     rng = np.random.default_rng(11)
     n_sub = min(len(p), args.ref_anchors)
     tri, tot_ms, k_ms = [], [], []
-    for i in range(args.warmup + args.steps):
-        sub = np.ascontiguousarray(p[rng.choice(len(p), n_sub, replace=False)])
+    for _ in range(args.steps):
+        sub = p if n_sub == len(p) else np.ascontiguousarray(p[rng.choice(len(p), n_sub, replace=False)])
         h, kms, tms = O.reference_count(box, edges, sub, p, p)
-        if i >= args.warmup:
-            tri.append(h.sum())
-            tot_ms.append(tms)
-            k_ms.append(kms)
+        tri.append(h.sum())
+        tot_ms.append(tms)
+        k_ms.append(kms)
     value = sum(tri) / (sum(tot_ms) / 1e3)
-    sample = (f"{n_sub} random anchors per step of the {len(p):,}-point catalogue (all points as p2/p3); "
-              f"reference source/device.cu kernel, unmodified, via oracle/ref_runner.cu")
+    sample = (f"{n_sub} random anchors per timed step of the {len(p):,}-point catalogue (all points as "
+              f"p2/p3); reference source/device.cu kernel, unmodified, on the GB300 via "
+              f"oracle/ref_runner.cu (the reference has no CPU counting path); warm-up steps: "
+              f"4096 anchors of the 20,000-point uniform box")
     return {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": sum(tot_ms) / len(tot_ms),
@@ -314,6 +338,7 @@ def run_reference(args) -> dict:
         "kernel_only": {"value": sum(tri) / (sum(k_ms) / 1e3), "unit": UNIT,
                         "ms_per_step": sum(k_ms) / len(k_ms)},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "reference",
+                         "device": "GB300 (the reference's CUDA kernel; one host thread drives it)",
                          "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -326,8 +351,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--workload", default="box_clustered",
-                    choices=["box_clustered", "box_uniform", "soneira_peebles"])
-    ap.add_argument("--ref-anchors", type=int, default=8192)
+                    choices=["box_clustered", "box_clustered_L1000", "box_uniform", "soneira_peebles"])
+    ap.add_argument("--ref-anchors", type=int, default=152 * 4 * 64)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--anchor-slab", type=float, default=None,
                     help="profiling size: anchors restricted to points with x < W (Mpc/h)")
