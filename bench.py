@@ -190,6 +190,41 @@ def barrier(world: int):
     torch.cuda.synchronize()
 
 
+def training_catalogue(name: str, i: int):
+    """Catalogue i of the work model's training set: the workload's process,
+    smaller, with its own seed."""
+    from cudancorr_gb300 import catalogs as C
+    if name == "soneira_peebles":
+        return C.training_soneira_peebles(i)
+    if name in ("box_clustered", "box_clustered_L1000"):
+        return C.neyman_scott(25000, 10.0, 2.0, 1000.0, 200 + i), 1000.0, C.linear_edges(100.0, 20)
+    raise SystemExit(f"no training process for workload {name}")
+
+
+def train_work_model(name: str, n_cat: int = 20):
+    """Trains the scheduler's work model on cell work measured by plain runs
+    (dynamic schedule) of n_cat training catalogues, on the GPU."""
+    from cudancorr_gb300 import api
+    t0 = time.perf_counter()
+    xs, ys = [], []
+    for i in range(n_cat):
+        q, qbox, qedges = training_catalogue(name, i)
+        with api.ncorr(np.full(3, qbox), api.threeD, qedges, False, (0.0, 0.0, 0.0)) as c:
+            c.set_record_work(True)
+            c.calculateD1D2D3(q, q, q)
+            f, w = c.cell_work()
+        keep = f[:, 0] > 0
+        xs.append(f[keep])
+        ys.append(np.log1p(w[keep]).astype(np.float32))
+    t1 = time.perf_counter()
+    x, y = np.concatenate(xs), np.concatenate(ys)
+    model = api.WorkModel(seed=1)
+    mse = model.train(x, y, epochs=200, batch=256, lr=3e-3, seed=2)
+    t2 = time.perf_counter()
+    return model, {"training_catalogues": n_cat, "training_cells": int(len(x)), "train_mse_log": mse,
+                   "s_measure": round(t1 - t0, 2), "s_train": round(t2 - t1, 2)}
+
+
 def run_engine(args) -> dict:
     import torch
     from cudancorr_gb300 import api
@@ -204,6 +239,12 @@ def run_engine(args) -> dict:
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.Stream(device=dev)
     corr = api.ncorr(np.full(3, box), api.threeD, edges, False, (0.0, 0.0, 0.0))
+    model, train_info = None, None
+    if args.schedule == "learned":
+        model, train_info = train_work_model(args.workload)
+        corr.set_schedule(api.SCHED_LEARNED, model)
+    elif args.schedule == "static":
+        corr.set_schedule(api.SCHED_STATIC)
 
     def device_step():
         with torch.cuda.stream(stream):
@@ -250,6 +291,32 @@ def run_engine(args) -> dict:
         _ = corr.getTriCountsOut()
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
     e2e_total = barrier_max(sum(e2e_ms), world)
+    h_main = corr.getTriCountsAll()
+
+    sched_cmp = None
+    if args.schedule == "learned":
+        # The same count under the other schedules (device-resident, one step
+        # each), the model's prediction error on this catalogue's cells, and
+        # the check that the counts do not depend on the schedule.
+        times, same = {"learned": statistics.mean(kernel_ms)}, True
+        for name, mode in (("dynamic", api.SCHED_DYNAMIC), ("static", api.SCHED_STATIC)):
+            corr.set_schedule(mode)
+            corr.set_record_work(name == "dynamic")
+            device_step()
+            times[name] = corr.stats()["ms_count"]
+            same = same and bool(np.array_equal(corr.getTriCountsAll(), h_main))
+            if name == "dynamic":
+                f, w = corr.cell_work()
+        corr.set_record_work(False)
+        keep = f[:, 0] > 0
+        y = np.log1p(w[keep])
+        pred = model.predict(f[keep]).astype(np.float64)
+        sched_cmp = {"kernel_ms": times, "speedup_vs_static": times["static"] / times["learned"],
+                     "speedup_vs_dynamic": times["dynamic"] / times["learned"], "counts_identical": same,
+                     "prediction": {"cells": int(keep.sum()), "mse_log": float(np.mean((pred - y) ** 2)),
+                                    "r2_log": float(1.0 - np.mean((pred - y) ** 2) / np.var(y)),
+                                    "total_work_rel_err": float(np.expm1(pred).sum() / np.expm1(y).sum() - 1.0)},
+                     "training": train_info}
     corr.close()
 
     sm_mhz = clocks.get("sm_mhz") or 1995.0
@@ -282,9 +349,125 @@ def run_engine(args) -> dict:
         "clocks": clocks,
         "exact_path": {"pairs": int(st_last["n_exact_pairs"]), "triangles": int(st_last["n_exact_tris"]),
                        "flagged_rows": int(st_last["n_flagged_rows"]), "queued": int(st_last["n_queued"])},
+        "schedule": args.schedule,
     }
+    if sched_cmp is not None:
+        out["schedules"] = sched_cmp
     if world == 1 and not args.no_cpu_baseline and args.anchor_slab is None:
         out["cpu_baseline"] = cpu_baseline(p, box, edges)
+    return out if rank == 0 else None
+
+
+def run_batch(args) -> dict:
+    """Batched mocks: 64 Neyman-Scott catalogues counted by one persistent
+    launch inside one CUDA graph (autotuned), against 64 separate
+    calculateD1D2D3 calls. Each rank counts its own 64 mocks."""
+    import torch
+    from cudancorr_gb300 import api
+    from cudancorr_gb300 import catalogs as C
+
+    world, rank, local = dist_setup()
+    mocks, box, edges = C.config_batch_mocks(seed=4 + rank)
+    desc = ("64 Neyman-Scott mocks, L=1000 Mpc/h, sizes log-uniform in [50,000, 1,000,000], N/8 parents "
+            "x Poisson(8), sigma 1.5, r_max=60 (17 cells, non-divisible), 12 linear bins, unweighted")
+    dev = torch.device("cuda", local)
+    t_mocks = [torch.from_numpy(m).to(dev) for m in mocks]
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    corr = api.ncorr(np.full(3, box), api.threeD, edges, False, (0.0, 0.0, 0.0))
+    sched = args.schedule
+    model, train_info = None, None
+    if sched == "learned":
+        raise SystemExit("batch_mocks: the learned schedule has no training process here; use dynamic or static")
+    if sched == "static":
+        corr.set_schedule(api.SCHED_STATIC)
+    b = api.Batch(corr, [(t, t, t) for t in t_mocks], autotune=not args.no_autotune)
+    plan = b.stats()
+
+    def step():
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        b.run()
+        return b.stats()
+
+    for _ in range(args.warmup):
+        step()
+    sampler = ClockSampler(local)
+    sampler.start()
+    barrier(world)
+    run_ms, count_ms, tri = [], [], []
+    for _ in range(args.steps):
+        st = step()
+        run_ms.append(st["ms_run"])
+        count_ms.append(st["ms_count"])
+        tri.append(st["triangles"])
+    barrier(world)
+    clocks = sampler.stop()
+    st_last = b.stats()
+    counts_batch = [b.counts_all(i) for i in range(len(mocks))]
+    b.close()
+    total_ms = barrier_max(sum(run_ms), world)
+    total_tri = barrier_sum(float(sum(tri)), world)
+
+    # 64 separate calls (device-resident), the plain method; counts must agree.
+    plain_ms, same = 0.0, True
+    for i, t in enumerate(t_mocks):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        corr._calculate_device(t, t, t)
+        plain_ms += (time.perf_counter() - t0) * 1e3
+        same = same and bool(np.array_equal(corr.getTriCountsAll(), counts_batch[i]))
+
+    # End to end: host arrays bound to a batch, copies inside the graph.
+    corr.set_tuning(plan["sub_j"], plan["hist_copies"])  # the device batch's autotuned choice
+    hb = api.Batch(corr, [(m, m, m) for m in mocks], autotune=False)
+    hb.run()
+    barrier(world)
+    e2e_ms = []
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        hb.run()
+        _ = [hb.counts_all(i) for i in range(len(mocks))]
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    hb.close()
+    corr.close()
+    e2e_total = barrier_max(sum(e2e_ms), world)
+
+    sm_mhz = clocks.get("sm_mhz") or 1995.0
+    peak_tflops = N_SM * FP32_LANES_PER_SM * 2 * sm_mhz * 1e6 / 1e12
+    flops = 8.0 * (st_last["n_pairs"] + st_last["n_pair_evals"])
+    achieved = flops / (statistics.mean(count_ms) / 1e3) / 1e12
+    nb = len(edges) - 1
+    n_pts = int(sum(len(m) for m in mocks))
+    out = {
+        "metric": METRIC, "value": total_tri / (total_ms / 1e3), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32+fp64-exact",
+        "data": "synthetic (seeded)",
+        "config": {"workload": "batch_mocks", "description": desc, "n_catalogues": len(mocks),
+                   "n_points": n_pts, "box": box, "r_max": float(edges[-1]), "bins_per_side": nb,
+                   "triangles_per_step": int(tri[-1]), "l2": "flushed (256 MiB write) between steps",
+                   "parallelism": f"{world} x 64 independent catalogues, one batch per GPU"},
+        "e2e": {"value": total_tri / (e2e_total / 1e3), "unit": UNIT,
+                "h2d_bytes_per_step": int(sum(m.nbytes for m in mocks)),
+                "d2h_bytes_per_step": int(len(mocks) * nb ** 3 * 8), "ms_per_step": e2e_total / args.steps},
+        "roofline": {"bound": "fp32_issue", "achieved": achieved, "peak": peak_tflops, "unit": "TFLOP/s",
+                     "frac": achieved / peak_tflops, "traffic": None, "kernel": "k_triangles",
+                     "kernel_ms": statistics.mean(count_ms),
+                     "work": "8 flops x (candidate triangles W + pair-stage evaluations P) per launch",
+                     "W": int(st_last["n_pairs"]), "P": int(st_last["n_pair_evals"]),
+                     "peak_basis": "152 SMs x 128 FP32 lanes x 2 x median sampled SM clock"},
+        "gpu_launches": int(plan["graph_nodes"]) * args.steps,
+        "clocks": clocks,
+        "batch": {"graph_nodes": plan["graph_nodes"], "ms_plan": plan["ms_plan"],
+                  "ms_autotune": plan["ms_autotune"], "tuning": {"sub_j": plan["sub_j"],
+                                                                 "hist_copies": plan["hist_copies"]},
+                  "grid_ctas": plan["grid_ctas"], "schedule": sched,
+                  "plain_64_calls_ms": plain_ms, "speedup_vs_plain": plain_ms / (total_ms / args.steps),
+                  "counts_identical_to_plain": same},
+    }
     return out if rank == 0 else None
 
 
@@ -309,6 +492,9 @@ def run_reference(args) -> dict:
         O.runner()
     except Exception as e:  # the cubin is built where the reference sources are mounted
         return {"impl": "reference", "unavailable": f"reference kernel not loadable: {e}"}
+    if args.workload == "batch_mocks":
+        return {"impl": "reference", "unavailable": "the reference arm times the single-catalogue workloads; "
+                                                    "batch_mocks would be 64 reference calls of hours each"}
     p, box, edges, desc = workload(args.workload, 0)
     from cudancorr_gb300 import catalogs as C
     wp, wbox, wedges = C.config_box_uniform()
@@ -351,7 +537,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--workload", default="box_clustered",
-                    choices=["box_clustered", "box_clustered_L1000", "box_uniform", "soneira_peebles"])
+                    choices=["box_clustered", "box_clustered_L1000", "box_uniform", "soneira_peebles",
+                             "batch_mocks"])
+    ap.add_argument("--schedule", default="dynamic", choices=["dynamic", "static", "learned"],
+                    help="anchor order of the triangle kernel (learned: trains the work model first)")
+    ap.add_argument("--no-autotune", action="store_true", help="batch_mocks: default tuning")
     ap.add_argument("--ref-anchors", type=int, default=152 * 4 * 64)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--anchor-slab", type=float, default=None,
@@ -359,6 +549,8 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         out = run_reference(args)
+    elif args.workload == "batch_mocks":
+        out = run_batch(args)
     else:
         out = run_engine(args)
     if out is not None:

@@ -40,7 +40,15 @@ EXPORTS = (
     "ncorr_get_pi_bins_out", "ncorr_get_tri_counts_out", "ncorr_get_tri_counts_all",
     "ncorr_get_stats", "ncorr_last_error", "survey_prep_cat", "survey_prep_cat2",
     "survey_convert_coordinates", "ncorr_logspace", "ncorr_count_noalloc",
+    "ncorr_set_schedule", "ncorr_set_tuning", "ncorr_set_record_work", "ncorr_num_cells",
+    "ncorr_get_cell_work", "ncorr_sched_create", "ncorr_sched_destroy", "ncorr_sched_num_params",
+    "ncorr_sched_get_params", "ncorr_sched_set_params", "ncorr_sched_predict", "ncorr_sched_gradient",
+    "ncorr_sched_train", "ncorr_batch_create", "ncorr_batch_run", "ncorr_batch_get_counts_all",
+    "ncorr_batch_get_stats", "ncorr_batch_destroy",
 )
+
+# Work-queue schedules (ncorr_set_schedule).
+SCHED_DYNAMIC, SCHED_STATIC, SCHED_LEARNED = 0, 1, 2
 
 
 class NcorrError(RuntimeError):
@@ -66,8 +74,23 @@ class NcorrStats(ctypes.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class NcorrBatchStats(ctypes.Structure):
+    _fields_ = [
+        ("ms_plan", ctypes.c_double), ("ms_autotune", ctypes.c_double), ("ms_run", ctypes.c_double),
+        ("ms_count", ctypes.c_double), ("n_work", ctypes.c_uint64), ("n_pairs", ctypes.c_uint64),
+        ("n_pair_evals", ctypes.c_uint64),
+        ("triangles", ctypes.c_uint64), ("n_items", ctypes.c_int), ("n_catalogues", ctypes.c_int),
+        ("sub_j", ctypes.c_int), ("hist_copies", ctypes.c_int), ("grid_ctas", ctypes.c_int),
+        ("weighted", ctypes.c_int), ("graph_nodes", ctypes.c_int),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 _LIB: Optional[ctypes.CDLL] = None
 _D = ctypes.POINTER(ctypes.c_double)
+_F = ctypes.POINTER(ctypes.c_float)
 
 
 def library_path() -> pathlib.Path:
@@ -108,6 +131,26 @@ def load_library() -> ctypes.CDLL:
         "survey_convert_coordinates": (i32, [_D, _D, i64, _D]),
         "ncorr_logspace": (i32, [ctypes.c_double, ctypes.c_double, i32, _D]),
         "ncorr_count_noalloc": (i32, [_D, _D, i32, i32, vp, i64, vp, i64, vp, i64, vp, vp]),
+        "ncorr_set_schedule": (i32, [vp, i32, vp]),
+        "ncorr_set_tuning": (i32, [vp, i32, i32]),
+        "ncorr_set_record_work": (i32, [vp, i32]),
+        "ncorr_num_cells": (i64, [vp]),
+        "ncorr_get_cell_work": (i32, [vp, _F, _D, i64]),
+        "ncorr_sched_create": (i32, [ctypes.c_uint64, hp]),
+        "ncorr_sched_destroy": (None, [vp]),
+        "ncorr_sched_num_params": (i32, []),
+        "ncorr_sched_get_params": (i32, [vp, _F, i64]),
+        "ncorr_sched_set_params": (i32, [vp, _F, i64]),
+        "ncorr_sched_predict": (i32, [vp, _F, i64, _F]),
+        "ncorr_sched_gradient": (i32, [vp, _F, _F, i64, _F, _F]),
+        "ncorr_sched_train": (i32, [vp, _F, _F, i64, i32, i32, ctypes.c_float, ctypes.c_uint64, _F]),
+        "ncorr_batch_create": (i32, [vp, i32, ctypes.POINTER(vp), ctypes.POINTER(i64), ctypes.POINTER(vp),
+                                     ctypes.POINTER(i64), ctypes.POINTER(vp), ctypes.POINTER(i64), i32, i32,
+                                     hp]),
+        "ncorr_batch_run": (i32, [vp, vp]),
+        "ncorr_batch_get_counts_all": (i32, [vp, i32, _D, i64]),
+        "ncorr_batch_get_stats": (i32, [vp, ctypes.POINTER(NcorrBatchStats)]),
+        "ncorr_batch_destroy": (None, [vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -247,6 +290,148 @@ class ncorr:
         s = NcorrStats()
         _check(self._lib.ncorr_get_stats(self._h, ctypes.byref(s)))
         return s.as_dict()
+
+    # -- scheduling (no counterpart in the reference; counts never depend on it)
+    def set_schedule(self, mode: int, model: Optional["WorkModel"] = None) -> None:
+        """SCHED_DYNAMIC (default), SCHED_STATIC, or SCHED_LEARNED with a WorkModel."""
+        self._model = model  # the handle uses the model's parameters in later calls
+        _check(self._lib.ncorr_set_schedule(self._h, int(mode), model._s if model is not None else None))
+
+    def set_tuning(self, sub_j: int = 32, hist_copies: int = 1) -> None:
+        _check(self._lib.ncorr_set_tuning(self._h, int(sub_j), int(hist_copies)))
+
+    def set_record_work(self, on: bool = True) -> None:
+        _check(self._lib.ncorr_set_record_work(self._h, int(bool(on))))
+
+    def cell_work(self):
+        """(features n_cells x 28 float32, candidate pairs per cell float64) of
+        the last call made with set_record_work(True)."""
+        n = int(self._lib.ncorr_num_cells(self._h))
+        feats = np.zeros((n, 28), dtype=np.float32)
+        work = np.zeros(n, dtype=np.float64)
+        _check(self._lib.ncorr_get_cell_work(self._h, feats.ctypes.data_as(_F), _dptr(work), n))
+        return feats, work
+
+
+class WorkModel:
+    """The scheduler's per-cell work MLP (28 -> 64 -> 64 -> 1, ReLU), with its
+    inference, gradient and Adam training run by the engine's kernels."""
+
+    def __init__(self, seed: int = 0):
+        self._lib = load_library()
+        self._s = ctypes.c_void_p()
+        _check(self._lib.ncorr_sched_create(ctypes.c_uint64(seed), ctypes.byref(self._s)))
+
+    @staticmethod
+    def num_params() -> int:
+        return int(load_library().ncorr_sched_num_params())
+
+    def close(self) -> None:
+        if getattr(self, "_s", None) and self._s.value:
+            self._lib.ncorr_sched_destroy(self._s)
+            self._s = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def get_params(self) -> np.ndarray:
+        out = np.zeros(self.num_params(), dtype=np.float32)
+        _check(self._lib.ncorr_sched_get_params(self._s, out.ctypes.data_as(_F), out.size))
+        return out
+
+    def set_params(self, p) -> None:
+        a = np.ascontiguousarray(np.asarray(p, dtype=np.float32))
+        _check(self._lib.ncorr_sched_set_params(self._s, a.ctypes.data_as(_F), a.size))
+
+    def predict(self, feats) -> np.ndarray:
+        x = np.ascontiguousarray(np.asarray(feats, dtype=np.float32).reshape(-1, 28))
+        out = np.zeros(x.shape[0], dtype=np.float32)
+        _check(self._lib.ncorr_sched_predict(self._s, x.ctypes.data_as(_F), x.shape[0], out.ctypes.data_as(_F)))
+        return out
+
+    def gradient(self, feats, target):
+        """(gradient of the mean squared error, sum of squared errors)."""
+        x = np.ascontiguousarray(np.asarray(feats, dtype=np.float32).reshape(-1, 28))
+        t = np.ascontiguousarray(np.asarray(target, dtype=np.float32).reshape(-1))
+        g = np.zeros(self.num_params(), dtype=np.float32)
+        loss = ctypes.c_float(0)
+        _check(self._lib.ncorr_sched_gradient(self._s, x.ctypes.data_as(_F), t.ctypes.data_as(_F), x.shape[0],
+                                              g.ctypes.data_as(_F), ctypes.byref(loss)))
+        return g, float(loss.value)
+
+    def train(self, feats, target, epochs: int = 30, batch: int = 512, lr: float = 3e-3, seed: int = 0) -> float:
+        """Adam on the GPU; returns the mean squared error after training."""
+        x = np.ascontiguousarray(np.asarray(feats, dtype=np.float32).reshape(-1, 28))
+        t = np.ascontiguousarray(np.asarray(target, dtype=np.float32).reshape(-1))
+        loss = ctypes.c_float(0)
+        _check(self._lib.ncorr_sched_train(self._s, x.ctypes.data_as(_F), t.ctypes.data_as(_F), x.shape[0],
+                                           int(epochs), int(batch), float(lr), ctypes.c_uint64(seed),
+                                           ctypes.byref(loss)))
+        return float(loss.value)
+
+
+class Batch:
+    """Many catalogue triples counted by one persistent launch inside one CUDA
+    graph (ncorr_batch_*). `items` is a sequence of (p1, p2, p3): numpy N x 4
+    float64 arrays (host) or CUDA float64 tensors (device). The arrays are
+    bound to the batch; run() counts their current contents."""
+
+    def __init__(self, corr: ncorr, items, autotune: bool = True):
+        lib = load_library()
+        self._lib = lib
+        self._corr = corr
+        keep, ptr, size = {}, [], []
+        on_device = None
+        for trip in items:
+            for p in trip:
+                dev = _is_cuda_tensor(p)
+                if on_device is None:
+                    on_device = dev
+                elif on_device != dev:
+                    raise NcorrError(NCORR_ERR_INVALID_ARGUMENT, "a batch is all host or all device arrays")
+                if id(p) not in keep:
+                    keep[id(p)] = p if dev else as_catalog(p)
+                a = keep[id(p)]
+                ptr.append(a.data_ptr() if dev else a.ctypes.data)
+                size.append(a.shape[0])
+        self._keep = keep
+        n = len(items)
+        vp_arr = ctypes.c_void_p * n
+        i64_arr = ctypes.c_int64 * n
+        p1 = vp_arr(*ptr[0::3]); p2 = vp_arr(*ptr[1::3]); p3 = vp_arr(*ptr[2::3])
+        n1 = i64_arr(*size[0::3]); n2 = i64_arr(*size[1::3]); n3 = i64_arr(*size[2::3])
+        self._b = ctypes.c_void_p()
+        self.n_items = n
+        _check(lib.ncorr_batch_create(corr._h, n, p1, n1, p2, n2, p3, n3, int(bool(on_device)),
+                                      int(bool(autotune)), ctypes.byref(self._b)))
+
+    def run(self, stream=None) -> None:
+        _check(self._lib.ncorr_batch_run(self._b, ctypes.c_void_p(stream) if stream is not None else None))
+
+    def counts_all(self, item: int) -> np.ndarray:
+        nb = self._corr.num_bins
+        out = np.zeros(nb ** 3, dtype=np.float64)
+        _check(self._lib.ncorr_batch_get_counts_all(self._b, int(item), _dptr(out), out.size))
+        return out
+
+    def stats(self) -> dict:
+        s = NcorrBatchStats()
+        _check(self._lib.ncorr_batch_get_stats(self._b, ctypes.byref(s)))
+        return s.as_dict()
+
+    def close(self) -> None:
+        if getattr(self, "_b", None) and self._b.value:
+            self._lib.ncorr_batch_destroy(self._b)
+            self._b = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def _is_cuda_tensor(x) -> bool:

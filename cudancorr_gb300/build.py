@@ -21,7 +21,7 @@ OUT = PKG / "lib"
 OBJ = PKG / "lib" / "obj"
 LIBNAME = "libcudancorr_gb300.so"
 
-SOURCES = ["cell_list.cu", "triangles_launch.cu", "capi.cu"]
+SOURCES = ["cell_list.cu", "triangles_launch.cu", "sched.cu", "capi.cu", "sched_api.cu", "batch.cu"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-Xptxas", "-warn-spills"]

@@ -111,3 +111,21 @@ def config_soneira_peebles(seed: int = 5, n_top: int = 3906):
     """Soneira-Peebles, 5 levels, eta=4, lambda=1.9, top radius 200,
     3906 top clumps (~4M points), L=1500, 16 linear bins on [0, 80)."""
     return soneira_peebles(n_top, 5, 4, 1.9, 200.0, 1500.0, seed), 1500.0, linear_edges(80.0, 16)
+
+
+def config_batch_mocks(seed: int = 4, n_mocks: int = 64, n_min: int = 50_000, n_max: int = 1_000_000):
+    """64 Neyman-Scott mocks in L=1000 with sizes log-uniform in
+    [50,000, 1,000,000]: N/8 parents, Poisson(8) children, sigma 1.5;
+    r_max=60 (17 cells, the last 40 wide), 12 linear bins."""
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(n_min), np.log(n_max), n_mocks))
+    mocks = [neyman_scott(max(1, int(round(s / 8.0))), 8.0, 1.5, 1000.0, seed * 1000 + i)
+             for i, s in enumerate(sizes)]
+    return mocks, 1000.0, linear_edges(60.0, 12)
+
+
+def training_soneira_peebles(index: int):
+    """Training catalogue `index` of the scheduler's work model: the 4M-point
+    Soneira-Peebles process at the same clump density in L=600 (250 top
+    clumps, 256,000 points), r_max=80, 16 linear bins."""
+    return soneira_peebles(250, 5, 4, 1.9, 200.0, 600.0, 100 + index), 600.0, linear_edges(80.0, 16)

@@ -1,238 +1,17 @@
 // C ABI of the engine (include/ncorr_gb300.h): handle life cycle, host
 // orchestration of one calculateD1D2D3, result compaction.
-#include <algorithm>
-#include <chrono>
-#include <cmath>
-#include <cstdlib>
-#include <cstring>
-#include <limits>
 #include <mutex>
-#include <string>
-#include <vector>
 
-#include "../../include/ncorr_gb300.h"
-#include "engine.cuh"
-#include "triangles.cuh"
-
-namespace ncorr_gb300 {
-void launch_assign(const double4_16a* in, int n, const Geom& g, int* cid, int* count, int* flags,
-                   unsigned* wmax_bits, cudaStream_t st);
-void launch_scan(const int* count, int ncell, int* start, int* cursor, cudaStream_t st);
-void launch_scatter(const double4_16a* in, int n, const Geom& g, const int* cid, int* cursor,
-                    double4_16a* pd, float4* pq, int* pc, cudaStream_t st);
-void launch_nbr_bound(const int* count, const Geom& g, int* out, cudaStream_t st);
-cudaError_t launch_triangles(const KArgs& a, bool survey, bool sym, bool weighted, bool hg, int grid,
-                             size_t smem, cudaStream_t st);
-int triangles_occupancy(bool survey, bool sym, bool weighted, bool hg, size_t smem);
-void launch_exact(const KArgs& a, bool survey, bool weighted, int grid, cudaStream_t st);
-void launch_fold(const unsigned long long* counts, const unsigned long long* wsum, int nb,
-                 bool weighted, double factor, double inv_scale, double* out,
-                 unsigned long long* total, cudaStream_t st);
-}  // namespace ncorr_gb300
+#include "host.cuh"
 
 using namespace ncorr_gb300;
+using namespace ncorr_host;
 
-namespace {
-
+namespace ncorr_host {
 thread_local std::string t_err;
-
-int fail(int code, const std::string& msg) {
-  t_err = msg;
-  return code;
-}
-
-// Contraction pattern of the reference's sqrSep as compiled by nvcc for the
-// GB300, established by running the reference kernel on inputs built to
-// separate the candidates: fma(dz, dz, fma(dx, dx, dy*dy)).
-constexpr int kDefaultFmaPattern = 2;
-
-// Budget of dynamic shared memory per CTA so that two CTAs share an SM, and
-// the largest CTA histogram kept in shared memory.
-constexpr int kSmemBudget = 110 * 1024;
-constexpr long kHistSmemMax = 56 * 1024;
-constexpr unsigned kExactQueueCap = 1u << 24;  // 16M entries, 256 MiB
-
-struct DevBuf {
-  void* p = nullptr;
-  size_t cap = 0;
-  cudaError_t ensure(size_t bytes) {
-    if (bytes <= cap && p) return cudaSuccess;
-    if (p) cudaFree(p);
-    p = nullptr;
-    cap = 0;
-    size_t b = std::max<size_t>(bytes, 256);
-    cudaError_t e = cudaMalloc(&p, b);
-    if (e == cudaSuccess) cap = b;
-    return e;
-  }
-  void release() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    cap = 0;
-  }
-  template <class T>
-  T* as() const {
-    return static_cast<T*>(p);
-  }
-};
-
-struct CatDev {
-  DevBuf in, cid, count, start, cursor, pd, pq, pc;
-  int n = 0;
-};
-
-}  // namespace
-
-struct ncorr_handle {
-  int survey = 0;
-  double box[3] = {0, 0, 0};
-  double ori[3] = {0, 0, 0};
-  std::vector<double> edges, mids;
-  int nb = 0;
-  long ncell = 0;
-  Geom g;
-  std::vector<unsigned char> table;
-  int table_scale = 0;  // code scale the uploaded table was built with
-  std::vector<double> counts_all, counts_out, tri_bins_out;
-  ncorr_stats stats;
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
-  CatDev cat[3];
-  DevBuf d_table, d_flags, d_wmax, d_work, d_bound, d_hist, d_out, d_stats, d_total;
-  DevBuf slab_e, slab_m, slab_p, slab_w;
-  DevBuf xq, xq_count;  // deferred exact candidates
-  DevBuf d_args;        // global copy of the triangle kernel's arguments
-  unsigned xq_cap = 0;
-  bool table_uploaded = false;
-};
+}  // namespace ncorr_host
 
 namespace {
-
-float f32_down(double x) {
-  float f = static_cast<float>(x);
-  if (static_cast<double>(f) > x) f = std::nextafter(f, -std::numeric_limits<float>::infinity());
-  return f;
-}
-float f32_up(double x) {
-  float f = static_cast<float>(x);
-  if (static_cast<double>(f) < x) f = std::nextafter(f, std::numeric_limits<float>::infinity());
-  return f;
-}
-
-// FP32 error model (u = 2^-24).
-//  * List entries hold d = fl32(D), D the exact anchor-relative offset
-//    (computed in FP64), |D| < r_max. The pair estimate a = fl32(|d|^2)
-//    satisfies |a - A| <= 5u A; the triangle estimate v = fl32(|d_j - d_l|^2)
-//    satisfies |v - V| <= 7u V + 2u r_max^2 (componentwise error
-//    u(|D_j| + |D_l| + |X|), Cauchy-Schwarz, AM-GM on the cross term, three
-//    roundings in the sum of squares). ka, kb bound both with margin, also
-//    covering the rounding of the band arithmetic itself.
-//  * The prefilter estimate from cell-local coordinates (error <= 5u*cell +
-//    u|D| per component) satisfies |v - V| <= 14u V + 9u r_max^2; only used
-//    to skip candidates that are certainly out of range (pa, pb).
-//  * Heron: with |x - X| <= ka x + kb for all three sides, the exact Heron
-//    product H = 4ab - (c-a-b)^2 moves by <= 2S(ka S + 3 kb), its FP32
-//    evaluation errs by <= 6u S^2, and H >= 8.3u c_max^2 proves that the
-//    reference's FP32 sqrtf test keeps the triangle. Hence the test
-//    H > S (ha S + hb).
-// Margins are generous on purpose: a wider band only sends more candidates
-// to the exact FP64 path.
-void set_error_model(Geom& g) {
-  const double u = std::ldexp(1.0, -24);
-  const double r2 = g.sqr_rmax;
-  g.ka = static_cast<float>(12.0 * u);
-  g.kb = static_cast<float>(4.0 * u * r2);
-  g.ha = static_cast<float>(48.0 * u);
-  g.hb = static_cast<float>(32.0 * u * r2);
-  // Prefilter thresholds: candidates with v >= pre_hi or v <= pre_lo are
-  // certainly outside (r_min^2, r_max^2).
-  const double eb = 20.0 * u, ec = 12.0 * u * r2;
-  g.pre_hi = f32_up((r2 + ec) / (1.0 - eb) * (1.0 + 4.0 * u));
-  g.pre_lo = f32_down((g.sqr_rmin - ec) / (1.0 + eb) * (1.0 - 4.0 * u) - 4.0 * u * ec);
-}
-
-// Bin table: entry i covers every v with rint(v * scale) == i. Its code is the
-// bin that contains the whole error band of every such v (times code_scale,
-// the byte stride of a bin in the CTA histogram), kCodeReject when the band
-// lies outside (rmin^2, rmax^2), or kCodeCareful otherwise.
-void build_table(Geom& g, int code_scale, std::vector<unsigned char>& tab) {
-  const int n = kTableSize;
-  tab.assign(n, static_cast<unsigned char>(kCodeCareful));
-  const double vmax = g.sqr_rmax * 1.05;
-  const float scale = static_cast<float>((n - 2) / vmax);
-  g.tab_scale = scale;
-  g.tab_n = n;
-  const double ka = g.ka, kb = g.kb;
-  for (int i = 0; i < n; ++i) {
-    double lo = (i - 0.5) / static_cast<double>(scale);
-    double hi = (i + 0.5) / static_cast<double>(scale);
-    if (lo < 0) lo = 0;
-    if (i == n - 1) hi = std::numeric_limits<double>::infinity();
-    // Inflate slightly for the rounding of the band arithmetic itself.
-    const double blo = lo - (ka * lo + kb) * 1.01;
-    const double bhi = hi + (ka * hi + kb) * 1.01;
-    unsigned char code = static_cast<unsigned char>(kCodeCareful);
-    if (bhi <= g.sqr_rmin || blo >= g.sqr_rmax) {
-      code = static_cast<unsigned char>(kCodeReject);
-    } else if (blo > g.sqr_rmin && bhi < g.sqr_rmax) {
-      for (int b = 0; b < g.nb; ++b) {
-        if (g.sqr_bins[b] <= blo && bhi < g.sqr_bins[b + 1]) {
-          code = static_cast<unsigned char>(b * code_scale);
-          break;
-        }
-      }
-    }
-    tab[i] = code;
-  }
-}
-
-#define CU(call)                                                              \
-  do {                                                                        \
-    cudaError_t e_ = (call);                                                  \
-    if (e_ != cudaSuccess)                                                    \
-      return fail(NCORR_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
-  } while (0)
-
-int validate_catalog_ptr(const double* p, int64_t n) {
-  if (n < 0) return fail(NCORR_ERR_INVALID_ARGUMENT, "negative catalogue size");
-  if (n > 0 && !p) return fail(NCORR_ERR_INVALID_ARGUMENT, "null catalogue");
-  if (n > (int64_t(1) << 30)) return fail(NCORR_ERR_INVALID_ARGUMENT, "catalogue larger than 2^30 points");
-  return NCORR_OK;
-}
-
-// Builds the cell list of one catalogue already in device memory.
-int grid_catalog(ncorr_handle* h, int ci, const double4_16a* d_in, int n, cudaStream_t st) {
-  CatDev& c = h->cat[ci];
-  c.n = n;
-  const size_t nn = static_cast<size_t>(std::max(n, 1));
-  CU(c.cid.ensure(nn * sizeof(int)));
-  CU(c.count.ensure(h->ncell * sizeof(int)));
-  CU(c.start.ensure((h->ncell + 1) * sizeof(int)));
-  CU(c.cursor.ensure(h->ncell * sizeof(int)));
-  CU(c.pd.ensure(nn * sizeof(double4_16a)));
-  CU(c.pq.ensure(nn * sizeof(float4)));
-  CU(c.pc.ensure(nn * sizeof(int)));
-  CU(cudaMemsetAsync(c.count.p, 0, h->ncell * sizeof(int), st));
-  launch_assign(d_in, n, h->g, c.cid.as<int>(), c.count.as<int>(), h->d_flags.as<int>() + ci,
-                h->d_wmax.as<unsigned>(), st);
-  launch_scan(c.count.as<int>(), static_cast<int>(h->ncell), c.start.as<int>(), c.cursor.as<int>(), st);
-  launch_scatter(d_in, n, h->g, c.cid.as<int>(), c.cursor.as<int>(), c.pd.as<double4_16a>(),
-                 c.pq.as<float4>(), c.pc.as<int>(), st);
-  CU(cudaGetLastError());
-  return NCORR_OK;
-}
-
-Catalog view(const CatDev& c) {
-  Catalog v;
-  v.pd = c.pd.as<double4_16a>();
-  v.pq = c.pq.as<float4>();
-  v.pc = c.pc.as<int>();
-  v.start = c.start.as<int>();
-  v.count = c.count.as<int>();
-  v.n = c.n;
-  return v;
-}
 
 void compact(ncorr_handle* h) {
   const int nb = h->nb;
@@ -344,16 +123,19 @@ int run(ncorr_handle* h, const double4_16a* d1, int n1, const double4_16a* d2, i
     h->table_scale = code_scale;
   }
 
-  // Shared-memory list capacity and overflow slabs.
+  // Histogram copies that fit, then the shared-memory list capacity and the
+  // overflow slabs.
+  int copies = hg ? 1 : h->hist_copies;
+  while (copies > 1 && static_cast<long>(copies) * nbin * elem > kHistSmemMax) copies >>= 1;
   int ks = 0;
   {
-    SmemLayout L0 = make_layout(h->nb, 0, sym, weighted, hg);
+    SmemLayout L0 = make_layout(h->nb, 0, sym, weighted, hg, copies);
     int per = (sym ? 1 : 2) * (16 + 4 + 4 + (weighted ? 4 : 0));
     ks = (kSmemBudget - L0.total) / per;
     ks = (ks / kTile) * kTile;
     if (ks < kTile) ks = kTile;
   }
-  SmemLayout L = make_layout(h->nb, ks, sym, weighted, hg);
+  SmemLayout L = make_layout(h->nb, ks, sym, weighted, hg, copies);
   const size_t smem = static_cast<size_t>(L.total);
   int occ = triangles_occupancy(h->survey != 0, sym, weighted, hg, smem);
   if (occ <= 0) return fail(NCORR_ERR_CUDA, "triangle kernel does not fit on the device");
@@ -375,23 +157,66 @@ int run(ncorr_handle* h, const double4_16a* d1, int n1, const double4_16a* d2, i
   CU(cudaMemsetAsync(h->d_work.p, 0, sizeof(int), st));
   CU(h->d_out.ensure(nbin * sizeof(double)));
 
+  // The call is a batch of one item.
+  BatchItem it;
+  std::memset(&it, 0, sizeof(it));
+  it.c1 = view(h->cat[role[0]]);
+  it.c2 = view(h->cat[role[1]]);
+  it.c3 = view(h->cat[role[2]]);
+  it.hist.counts = weighted ? nullptr : h->d_hist.as<unsigned long long>();
+  it.hist.wsum = weighted ? h->d_hist.as<unsigned long long>() : nullptr;
+  it.out = h->d_out.as<double>();
+  it.total = h->d_total.as<unsigned long long>();
+  it.flags1 = h->d_flags.as<int>() + role[0];
+  it.sym6_ok = sym6 ? 1 : 0;
+  it.cell_base = 0;
+  CU(h->d_items.ensure(sizeof(BatchItem)));
+  CU(cudaMemcpyAsync(h->d_items.p, &it, sizeof(it), cudaMemcpyHostToDevice, st));
+
   KArgs a;
+  std::memset(&a, 0, sizeof(a));
   a.g = h->g;
-  a.c1 = view(h->cat[role[0]]);
-  a.c2 = view(h->cat[role[1]]);
-  a.c3 = view(h->cat[role[2]]);
+  a.items = h->d_items.as<BatchItem>();
+  a.n_items = 1;
+  a.n_work = n1;
+  a.q_item = nullptr;
+  a.q_anchor = nullptr;
+  a.sched_static = h->sched_mode == NCORR_SCHED_STATIC ? 1 : 0;
+  a.sub_j = h->sub_j;
+  a.hist_copies = copies;
+  a.cell_work = nullptr;
+  const bool need_feats = h->record_work || h->sched_mode == NCORR_SCHED_LEARNED;
+  if (need_feats) {
+    CU(h->d_feats.ensure(static_cast<size_t>(h->ncell) * kMlpIn * sizeof(float)));
+    launch_cell_features(a.items, 1, h->g, h->d_feats.as<float>(), st);
+  }
+  if (h->sched_mode == NCORR_SCHED_LEARNED && n1 > 0) {
+    // Cells heaviest first, as the work model predicts them.
+    OrderScratch os;
+    CU(h->order.ensure(1, h->ncell, &os));
+    CU(h->q_item.ensure(static_cast<size_t>(n1) * sizeof(int)));
+    CU(h->q_anchor.ensure(static_cast<size_t>(n1) * sizeof(int)));
+    launch_mlp_predict(h->sched_model->params.as<float>(), h->d_feats.as<float>(), static_cast<int>(h->ncell),
+                       os.pred, st);
+    launch_learned_queue(a.items, 1, static_cast<int>(h->ncell), os, h->q_item.as<int>(), h->q_anchor.as<int>(),
+                         st);
+    a.q_item = h->q_item.as<int>();
+    a.q_anchor = h->q_anchor.as<int>();
+  }
+  if (h->record_work) {
+    CU(h->d_cell_work.ensure(static_cast<size_t>(h->ncell) * sizeof(unsigned long long)));
+    CU(cudaMemsetAsync(h->d_cell_work.p, 0, static_cast<size_t>(h->ncell) * sizeof(unsigned long long), st));
+    a.cell_work = h->d_cell_work.as<unsigned long long>();
+  }
   a.table = h->d_table.as<unsigned char>();
   a.work = h->d_work.as<int>();
   a.flags = h->d_flags.as<int>() + 4;
-  a.hist.counts = weighted ? nullptr : h->d_hist.as<unsigned long long>();
-  a.hist.wsum = weighted ? h->d_hist.as<unsigned long long>() : nullptr;
   a.slab_e = h->slab_e.as<float4>();
   a.slab_m = h->slab_m.as<unsigned>();
   a.slab_p = h->slab_p.as<int>();
   a.slab_w = weighted ? h->slab_w.as<float>() : nullptr;
   a.ks = ks;
   a.kg = kg;
-  a.sym6 = sym6 ? 1 : 0;
   a.code_scale = code_scale;
   a.wscale = wscale;
   a.stats = h->d_stats.as<unsigned long long>();
@@ -411,10 +236,19 @@ int run(ncorr_handle* h, const double4_16a* d1, int n1, const double4_16a* d2, i
   if (n1 > 0) CU(launch_triangles(a, h->survey != 0, sym, weighted, hg, grid, smem, st));
   if (n1 > 0) launch_exact(a, h->survey != 0, weighted, nsm * 4, st);
   CU(cudaEventRecord(h->ev[3], st));
-  launch_fold(a.hist.counts, a.hist.wsum, h->nb, weighted, sym6 ? 6.0 : (sym ? 2.0 : 1.0), 1.0 / wscale,
-              h->d_out.as<double>(), h->d_total.as<unsigned long long>(), st);
+  launch_fold(a.items, 1, h->nb, weighted, sym, 1.0 / wscale, st);
   CU(cudaGetLastError());
   h->counts_all.assign(nbin, 0.0);
+  if (h->record_work) {
+    h->rec_feats.resize(static_cast<size_t>(h->ncell) * kMlpIn);
+    std::vector<unsigned long long> w(h->ncell);
+    CU(cudaMemcpyAsync(h->rec_feats.data(), h->d_feats.p, h->rec_feats.size() * sizeof(float),
+                       cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(w.data(), h->d_cell_work.p, w.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                       st));
+    CU(cudaStreamSynchronize(st));
+    h->rec_work.assign(w.begin(), w.end());
+  }
   unsigned long long st_host[8];
   unsigned long long total = 0;
   int kflags = 0;
@@ -577,8 +411,10 @@ void ncorr_destroy(ncorr_handle* h) {
   }
   for (DevBuf* b : {&h->d_table, &h->d_flags, &h->d_wmax, &h->d_work, &h->d_bound, &h->d_hist,
                     &h->d_out, &h->d_stats, &h->d_total, &h->slab_e, &h->slab_m, &h->slab_p,
-                    &h->slab_w, &h->xq, &h->xq_count, &h->d_args})
+                    &h->slab_w, &h->xq, &h->xq_count, &h->d_args, &h->d_items, &h->d_cell_work,
+                    &h->d_feats, &h->q_item, &h->q_anchor})
     b->release();
+  h->order.release();
   for (auto& e : h->ev)
     if (e) cudaEventDestroy(e);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -667,6 +503,47 @@ int ncorr_get_tri_counts_all(const ncorr_handle* h, double* out, int64_t cap) {
   if (cap < static_cast<int64_t>(h->counts_all.size()))
     return fail(NCORR_ERR_INVALID_ARGUMENT, "output capacity too small");
   std::memcpy(out, h->counts_all.data(), h->counts_all.size() * sizeof(double));
+  return NCORR_OK;
+}
+
+int ncorr_set_schedule(ncorr_handle* h, int mode, const ncorr_sched* model) {
+  if (!h) return fail(NCORR_ERR_INVALID_ARGUMENT, "null handle");
+  if (mode != NCORR_SCHED_DYNAMIC && mode != NCORR_SCHED_STATIC && mode != NCORR_SCHED_LEARNED)
+    return fail(NCORR_ERR_INVALID_ARGUMENT, "unknown schedule");
+  if (mode == NCORR_SCHED_LEARNED && !model)
+    return fail(NCORR_ERR_INVALID_ARGUMENT, "the learned schedule needs a model");
+  if (model && model->device != h->device)
+    return fail(NCORR_ERR_INVALID_ARGUMENT, "scheduler model belongs to another device");
+  h->sched_mode = mode;
+  h->sched_model = mode == NCORR_SCHED_LEARNED ? model : nullptr;
+  return NCORR_OK;
+}
+
+int ncorr_set_tuning(ncorr_handle* h, int sub_j, int hist_copies) {
+  if (!h) return fail(NCORR_ERR_INVALID_ARGUMENT, "null handle");
+  if (sub_j != 8 && sub_j != 16 && sub_j != 32) return fail(NCORR_ERR_INVALID_ARGUMENT, "sub_j must be 8, 16 or 32");
+  if (hist_copies != 1 && hist_copies != 2 && hist_copies != 4)
+    return fail(NCORR_ERR_INVALID_ARGUMENT, "hist_copies must be 1, 2 or 4");
+  h->sub_j = sub_j;
+  h->hist_copies = hist_copies;
+  return NCORR_OK;
+}
+
+int ncorr_set_record_work(ncorr_handle* h, int on) {
+  if (!h) return fail(NCORR_ERR_INVALID_ARGUMENT, "null handle");
+  h->record_work = on != 0;
+  return NCORR_OK;
+}
+
+int64_t ncorr_num_cells(const ncorr_handle* h) { return h ? static_cast<int64_t>(h->ncell) : 0; }
+
+int ncorr_get_cell_work(const ncorr_handle* h, float* feats, double* work, int64_t cap_cells) {
+  if (!h) return fail(NCORR_ERR_INVALID_ARGUMENT, "null handle");
+  if (h->rec_work.size() != static_cast<size_t>(h->ncell))
+    return fail(NCORR_ERR_INVALID_ARGUMENT, "no recorded call (ncorr_set_record_work)");
+  if (cap_cells < h->ncell) return fail(NCORR_ERR_INVALID_ARGUMENT, "output too small");
+  if (feats) std::memcpy(feats, h->rec_feats.data(), h->rec_feats.size() * sizeof(float));
+  if (work) std::memcpy(work, h->rec_work.data(), h->rec_work.size() * sizeof(double));
   return NCORR_OK;
 }
 
@@ -841,7 +718,7 @@ extern "C" int ncorr_count_noalloc(const double box[3], const double* edges, int
                                    const double* d_p1, int64_t n1, const double* d_p2, int64_t n2,
                                    const double* d_p3, int64_t n3, double* d_counts_all, void* stream) {
   static_assert(3 * kNoAllocCatBytes + kNoAllocHistBytes + kTableSize + kNoAllocExactCap * sizeof(ExactEntry) +
-                        sizeof(KArgs) + 64 * 1024 <= kNoAllocBytes,
+                        sizeof(KArgs) + sizeof(BatchItem) + 64 * 1024 <= kNoAllocBytes,
                 "scratch layout exceeds the scratch array");
   if (!box || !edges || !d_counts_all) return fail(NCORR_ERR_INVALID_ARGUMENT, "null box, edges or output");
   if (n_edges < 2 || n_edges - 1 > kNoAllocMaxBins)
@@ -928,6 +805,7 @@ extern "C" int ncorr_count_noalloc(const double box[3], const double* edges, int
   unsigned char* table = take(kTableSize);
   ExactEntry* xq = reinterpret_cast<ExactEntry*>(take(kNoAllocExactCap * sizeof(ExactEntry)));
   KArgs* d_args = reinterpret_cast<KArgs*>(take(sizeof(KArgs)));
+  BatchItem* d_item = reinterpret_cast<BatchItem*>(take(sizeof(BatchItem)));
   int* flags = reinterpret_cast<int*>(take(8 * sizeof(int)));
   unsigned* wmax = reinterpret_cast<unsigned*>(take(sizeof(unsigned)));
   int* work = reinterpret_cast<int*>(take(sizeof(int)));
@@ -1052,9 +930,6 @@ extern "C" int ncorr_count_noalloc(const double box[3], const double* edges, int
   CU(cudaMemcpyAsync(table, tab_host, kTableSize, cudaMemcpyHostToDevice, st));
   CU(cudaMemsetAsync(hist, 0, (weighted ? 2 : 1) * static_cast<size_t>(nbin) * sizeof(unsigned long long), st));
 
-  KArgs a;
-  std::memset(&a, 0, sizeof(a));
-  a.g = g;
   auto catview = [&](int ci, int64_t n) {
     Catalog v;
     v.pd = cat[ci].pd;
@@ -1065,21 +940,35 @@ extern "C" int ncorr_count_noalloc(const double box[3], const double* edges, int
     v.n = static_cast<int>(n);
     return v;
   };
-  a.c1 = catview(role[0], n1);
-  a.c2 = catview(role[1], n2);
-  a.c3 = catview(role[2], n3);
+  BatchItem it;
+  std::memset(&it, 0, sizeof(it));
+  it.c1 = catview(role[0], n1);
+  it.c2 = catview(role[1], n2);
+  it.c3 = catview(role[2], n3);
+  it.hist.counts = weighted ? nullptr : hist;
+  it.hist.wsum = weighted ? hist : nullptr;
+  it.out = d_counts_all;
+  it.total = total;
+  it.flags1 = flags + role[0];
+  it.sym6_ok = sym6 ? 1 : 0;
+  CU(cudaMemcpyAsync(d_item, &it, sizeof(it), cudaMemcpyHostToDevice, st));
+  KArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.g = g;
+  a.items = d_item;
+  a.n_items = 1;
+  a.n_work = static_cast<int>(n1);
+  a.sub_j = kSubJDefault;
+  a.hist_copies = 1;
   a.table = table;
   a.work = work;
   a.flags = flags + 4;
-  a.hist.counts = weighted ? nullptr : hist;
-  a.hist.wsum = weighted ? hist : nullptr;
   a.slab_e = reinterpret_cast<float4*>(slab);
   a.slab_m = reinterpret_cast<unsigned*>(slab);
   a.slab_p = reinterpret_cast<int*>(slab);
   a.slab_w = weighted ? reinterpret_cast<float*>(slab) : nullptr;
   a.ks = ks;
   a.kg = 0;
-  a.sym6 = sym6 ? 1 : 0;
   a.code_scale = code_scale;
   a.wscale = wscale;
   a.stats = stats;
@@ -1092,8 +981,7 @@ extern "C" int ncorr_count_noalloc(const double box[3], const double* edges, int
     CU(launch_triangles(a, g.survey != 0, sym, weighted, hg, grid, smem, st));
     launch_exact(a, g.survey != 0, weighted, nsm * 4, st);
   }
-  launch_fold(a.hist.counts, a.hist.wsum, g.nb, weighted, sym6 ? 6.0 : (sym ? 2.0 : 1.0), 1.0 / wscale,
-              d_counts_all, total, st);
+  launch_fold(d_item, 1, g.nb, weighted, sym, 1.0 / wscale, st);
   CU(cudaGetLastError());
   int kflags = 0;
   CU(cudaMemcpyAsync(&kflags, flags + 4, sizeof(int), cudaMemcpyDeviceToHost, st));

@@ -72,7 +72,8 @@ struct Catalog {
 };
 
 // A candidate triangle whose FP32 classification stays uncertain, deferred to
-// the exact FP64 kernel: anchor (sorted index in catalogue 1), the two
+// the exact FP64 kernel: the anchor's position in the work queue (which names
+// the batch item and the anchor's sorted index in its catalogue 1), the two
 // neighbours (sorted indices in catalogues 2 and 3), and
 // meta = slot_j | slot_l << 5 | bin_j << 10 | bin_l << 18.
 struct ExactEntry {
@@ -86,6 +87,25 @@ struct HistOut {
   unsigned long long* counts;  // nb^3 unsorted keys (count mode)
   unsigned long long* wsum;    // 2*nb^3 (weighted mode)
 };
+
+// One catalogue triple (p1, p2, p3) counted into its own histogram; a single
+// calculateD1D2D3 is a batch of one item. Items of one launch share the
+// geometry, the bins and the kernel variant (survey, p2 == p3, weighted).
+struct BatchItem {
+  Catalog c1, c2, c3;
+  HistOut hist;
+  double* out;                // folded nb^3 result (triCountsAll_ layout)
+  unsigned long long* total;  // sum of the folded unweighted counts
+  const int* flags1;          // grid flags of catalogue 1, read on the device
+  int sym6_ok;                // the host-side conditions of the six-fold loop hold
+  int cell_base;              // offset of this item's cells in per-cell arrays
+};
+
+// The six-fold loop runs for an item when the host allowed it and no point of
+// catalogue 1 broke the per-point conditions while it was gridded.
+__device__ __forceinline__ bool item_sym6(const BatchItem& it) {
+  return it.sym6_ok && !(*it.flags1 & kFlagNoSym6);
+}
 
 // Sum of squares of the reference's sqrSep (source/device.cu:30-36) under
 // the contraction pattern the CUDA compiler applied to it; the explicit

@@ -1,0 +1,291 @@
+// Host-side pieces shared by the C ABI translation units: error reporting,
+// device buffers, the handle, the FP32 error model and the bin table.
+#pragma once
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <vector>
+
+#include "../../include/ncorr_gb300.h"
+#include "engine.cuh"
+#include "sched.cuh"
+#include "triangles.cuh"
+
+namespace ncorr_gb300 {
+void launch_assign(const double4_16a* in, int n, const Geom& g, int* cid, int* count, int* flags,
+                   unsigned* wmax_bits, cudaStream_t st);
+void launch_scan(const int* count, int ncell, int* start, int* cursor, cudaStream_t st);
+void launch_scatter(const double4_16a* in, int n, const Geom& g, const int* cid, int* cursor,
+                    double4_16a* pd, float4* pq, int* pc, cudaStream_t st);
+void launch_nbr_bound(const int* count, const Geom& g, int* out, cudaStream_t st);
+cudaError_t launch_triangles(const KArgs& a, bool survey, bool sym, bool weighted, bool hg, int grid,
+                             size_t smem, cudaStream_t st, bool set_attr = true);
+int triangles_occupancy(bool survey, bool sym, bool weighted, bool hg, size_t smem);
+void launch_exact(const KArgs& a, bool survey, bool weighted, int grid, cudaStream_t st);
+void launch_fold(const BatchItem* items, int n_items, int nb, bool weighted, bool sym, double inv_scale,
+                 cudaStream_t st);
+}  // namespace ncorr_gb300
+
+namespace ncorr_host {
+
+using namespace ncorr_gb300;
+
+// Message of the last failed call on this thread (ncorr_last_error).
+extern thread_local std::string t_err;
+
+inline int fail(int code, const std::string& msg) {
+  t_err = msg;
+  return code;
+}
+
+// Contraction pattern of the reference's sqrSep as compiled by nvcc for the
+// GB300, established by running the reference kernel on inputs built to
+// separate the candidates: fma(dz, dz, fma(dx, dx, dy*dy)).
+constexpr int kDefaultFmaPattern = 2;
+
+// Budget of dynamic shared memory per CTA so that two CTAs share an SM, and
+// the largest CTA histogram kept in shared memory.
+constexpr int kSmemBudget = 110 * 1024;
+constexpr long kHistSmemMax = 56 * 1024;
+constexpr unsigned kExactQueueCap = 1u << 24;  // 16M entries, 256 MiB
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= cap && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t b = std::max<size_t>(bytes, 256);
+    cudaError_t e = cudaMalloc(&p, b);
+    if (e == cudaSuccess) cap = b;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+  template <class T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+};
+
+struct CatDev {
+  DevBuf in, cid, count, start, cursor, pd, pq, pc;
+  int n = 0;
+};
+
+// Device scratch of the learned queue order (OrderScratch), grown on demand.
+struct OrderBufs {
+  DevBuf pred, item_total, item_rank, ekey, kcount, kstart, kcursor, sorted, acount, aoff, acursor;
+  cudaError_t ensure(int n_items, long ncell, OrderScratch* out) {
+    const size_t m = static_cast<size_t>(n_items) * ncell;
+    const size_t nk = static_cast<size_t>(n_items) * kSchedBuckets + 1;
+    cudaError_t e;
+    if ((e = pred.ensure(m * sizeof(float))) || (e = item_total.ensure(n_items * sizeof(double))) ||
+        (e = item_rank.ensure(n_items * sizeof(int))) || (e = ekey.ensure(m * sizeof(int))) ||
+        (e = kcount.ensure(nk * sizeof(int))) || (e = kstart.ensure(nk * sizeof(int))) ||
+        (e = kcursor.ensure(nk * sizeof(int))) || (e = sorted.ensure(m * sizeof(int))) ||
+        (e = acount.ensure((m + 1) * sizeof(int))) || (e = aoff.ensure((m + 1) * sizeof(int))) ||
+        (e = acursor.ensure((m + 1) * sizeof(int))))
+      return e;
+    out->pred = pred.as<float>();
+    out->item_total = item_total.as<double>();
+    out->item_rank = item_rank.as<int>();
+    out->ekey = ekey.as<int>();
+    out->kcount = kcount.as<int>();
+    out->kstart = kstart.as<int>();
+    out->kcursor = kcursor.as<int>();
+    out->sorted = sorted.as<int>();
+    out->acount = acount.as<int>();
+    out->aoff = aoff.as<int>();
+    out->acursor = acursor.as<int>();
+    return cudaSuccess;
+  }
+  void release() {
+    for (DevBuf* b : {&pred, &item_total, &item_rank, &ekey, &kcount, &kstart, &kcursor, &sorted, &acount, &aoff,
+                      &acursor})
+      b->release();
+  }
+};
+
+}  // namespace ncorr_host
+
+struct ncorr_handle {
+  int survey = 0;
+  double box[3] = {0, 0, 0};
+  double ori[3] = {0, 0, 0};
+  std::vector<double> edges, mids;
+  int nb = 0;
+  long ncell = 0;
+  ncorr_gb300::Geom g;
+  std::vector<unsigned char> table;
+  int table_scale = 0;  // code scale the uploaded table was built with
+  std::vector<double> counts_all, counts_out, tri_bins_out;
+  ncorr_stats stats;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  ncorr_host::CatDev cat[3];
+  ncorr_host::DevBuf d_table, d_flags, d_wmax, d_work, d_bound, d_hist, d_out, d_stats, d_total;
+  ncorr_host::DevBuf slab_e, slab_m, slab_p, slab_w;
+  ncorr_host::DevBuf xq, xq_count;  // deferred exact candidates
+  ncorr_host::DevBuf d_args;        // global copy of the triangle kernel's arguments
+  unsigned xq_cap = 0;
+  bool table_uploaded = false;
+  // Work queue (ncorr_set_schedule, ncorr_set_tuning, ncorr_set_record_work).
+  int sched_mode = NCORR_SCHED_DYNAMIC;
+  const ncorr_sched* sched_model = nullptr;
+  int sub_j = ncorr_gb300::kSubJDefault;
+  int hist_copies = 1;
+  bool record_work = false;
+  ncorr_host::DevBuf d_items, d_cell_work, d_feats, q_item, q_anchor;
+  ncorr_host::OrderBufs order;
+  std::vector<float> rec_feats;   // features of the last recorded call, ncell x 28
+  std::vector<double> rec_work;   // its candidate pairs per cell of catalogue 1
+};
+
+// The scheduler's work-prediction MLP: parameters, Adam state and training
+// scratch on one device.
+struct ncorr_sched {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int step = 0;  // Adam steps taken
+  ncorr_host::DevBuf params, m, v, grad, loss, partial, partial_loss, feats, target, idx, pred;
+};
+
+namespace ncorr_host {
+
+inline float f32_down(double x) {
+  float f = static_cast<float>(x);
+  if (static_cast<double>(f) > x) f = std::nextafter(f, -std::numeric_limits<float>::infinity());
+  return f;
+}
+inline float f32_up(double x) {
+  float f = static_cast<float>(x);
+  if (static_cast<double>(f) < x) f = std::nextafter(f, std::numeric_limits<float>::infinity());
+  return f;
+}
+
+// FP32 error model (u = 2^-24).
+//  * List entries hold d = fl32(D), D the exact anchor-relative offset
+//    (computed in FP64), |D| < r_max. The pair estimate a = fl32(|d|^2)
+//    satisfies |a - A| <= 5u A; the triangle estimate v = fl32(|d_j - d_l|^2)
+//    satisfies |v - V| <= 7u V + 2u r_max^2 (componentwise error
+//    u(|D_j| + |D_l| + |X|), Cauchy-Schwarz, AM-GM on the cross term, three
+//    roundings in the sum of squares). ka, kb bound both with margin, also
+//    covering the rounding of the band arithmetic itself.
+//  * The prefilter estimate from cell-local coordinates (error <= 5u*cell +
+//    u|D| per component) satisfies |v - V| <= 14u V + 9u r_max^2; only used
+//    to skip candidates that are certainly out of range (pa, pb).
+//  * Heron: with |x - X| <= ka x + kb for all three sides, the exact Heron
+//    product H = 4ab - (c-a-b)^2 moves by <= 2S(ka S + 3 kb), its FP32
+//    evaluation errs by <= 6u S^2, and H >= 8.3u c_max^2 proves that the
+//    reference's FP32 sqrtf test keeps the triangle. Hence the test
+//    H > S (ha S + hb).
+// Margins are generous on purpose: a wider band only sends more candidates
+// to the exact FP64 path.
+inline void set_error_model(Geom& g) {
+  const double u = std::ldexp(1.0, -24);
+  const double r2 = g.sqr_rmax;
+  g.ka = static_cast<float>(12.0 * u);
+  g.kb = static_cast<float>(4.0 * u * r2);
+  g.ha = static_cast<float>(48.0 * u);
+  g.hb = static_cast<float>(32.0 * u * r2);
+  // Prefilter thresholds: candidates with v >= pre_hi or v <= pre_lo are
+  // certainly outside (r_min^2, r_max^2).
+  const double eb = 20.0 * u, ec = 12.0 * u * r2;
+  g.pre_hi = f32_up((r2 + ec) / (1.0 - eb) * (1.0 + 4.0 * u));
+  g.pre_lo = f32_down((g.sqr_rmin - ec) / (1.0 + eb) * (1.0 - 4.0 * u) - 4.0 * u * ec);
+}
+
+// Bin table: entry i covers every v with rint(v * scale) == i. Its code is the
+// bin that contains the whole error band of every such v (times code_scale,
+// the byte stride of a bin in the CTA histogram), kCodeReject when the band
+// lies outside (rmin^2, rmax^2), or kCodeCareful otherwise.
+inline void build_table(Geom& g, int code_scale, std::vector<unsigned char>& tab) {
+  const int n = kTableSize;
+  tab.assign(n, static_cast<unsigned char>(kCodeCareful));
+  const double vmax = g.sqr_rmax * 1.05;
+  const float scale = static_cast<float>((n - 2) / vmax);
+  g.tab_scale = scale;
+  g.tab_n = n;
+  const double ka = g.ka, kb = g.kb;
+  for (int i = 0; i < n; ++i) {
+    double lo = (i - 0.5) / static_cast<double>(scale);
+    double hi = (i + 0.5) / static_cast<double>(scale);
+    if (lo < 0) lo = 0;
+    if (i == n - 1) hi = std::numeric_limits<double>::infinity();
+    // Inflate slightly for the rounding of the band arithmetic itself.
+    const double blo = lo - (ka * lo + kb) * 1.01;
+    const double bhi = hi + (ka * hi + kb) * 1.01;
+    unsigned char code = static_cast<unsigned char>(kCodeCareful);
+    if (bhi <= g.sqr_rmin || blo >= g.sqr_rmax) {
+      code = static_cast<unsigned char>(kCodeReject);
+    } else if (blo > g.sqr_rmin && bhi < g.sqr_rmax) {
+      for (int b = 0; b < g.nb; ++b) {
+        if (g.sqr_bins[b] <= blo && bhi < g.sqr_bins[b + 1]) {
+          code = static_cast<unsigned char>(b * code_scale);
+          break;
+        }
+      }
+    }
+    tab[i] = code;
+  }
+}
+
+#define CU(call)                                                              \
+  do {                                                                        \
+    cudaError_t e_ = (call);                                                  \
+    if (e_ != cudaSuccess)                                                    \
+      return fail(NCORR_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+inline int validate_catalog_ptr(const double* p, int64_t n) {
+  if (n < 0) return fail(NCORR_ERR_INVALID_ARGUMENT, "negative catalogue size");
+  if (n > 0 && !p) return fail(NCORR_ERR_INVALID_ARGUMENT, "null catalogue");
+  if (n > (int64_t(1) << 30)) return fail(NCORR_ERR_INVALID_ARGUMENT, "catalogue larger than 2^30 points");
+  return NCORR_OK;
+}
+
+// Builds the cell list of one catalogue already in device memory.
+inline int grid_catalog(ncorr_handle* h, int ci, const double4_16a* d_in, int n, cudaStream_t st) {
+  CatDev& c = h->cat[ci];
+  c.n = n;
+  const size_t nn = static_cast<size_t>(std::max(n, 1));
+  CU(c.cid.ensure(nn * sizeof(int)));
+  CU(c.count.ensure(h->ncell * sizeof(int)));
+  CU(c.start.ensure((h->ncell + 1) * sizeof(int)));
+  CU(c.cursor.ensure(h->ncell * sizeof(int)));
+  CU(c.pd.ensure(nn * sizeof(double4_16a)));
+  CU(c.pq.ensure(nn * sizeof(float4)));
+  CU(c.pc.ensure(nn * sizeof(int)));
+  CU(cudaMemsetAsync(c.count.p, 0, h->ncell * sizeof(int), st));
+  launch_assign(d_in, n, h->g, c.cid.as<int>(), c.count.as<int>(), h->d_flags.as<int>() + ci,
+                h->d_wmax.as<unsigned>(), st);
+  launch_scan(c.count.as<int>(), static_cast<int>(h->ncell), c.start.as<int>(), c.cursor.as<int>(), st);
+  launch_scatter(d_in, n, h->g, c.cid.as<int>(), c.cursor.as<int>(), c.pd.as<double4_16a>(),
+                 c.pq.as<float4>(), c.pc.as<int>(), st);
+  CU(cudaGetLastError());
+  return NCORR_OK;
+}
+
+inline Catalog view(const CatDev& c) {
+  Catalog v;
+  v.pd = c.pd.as<double4_16a>();
+  v.pq = c.pq.as<float4>();
+  v.pc = c.pc.as<int>();
+  v.start = c.start.as<int>();
+  v.count = c.count.as<int>();
+  v.n = c.n;
+  return v;
+}
+
+}  // namespace ncorr_host

@@ -2,8 +2,12 @@
 // countTrianglesThreeDBox / countTrianglesThreeDSurvey
 // (source/device.cu:259-315, :381-431).
 //
-// One CTA of 256 threads owns one anchor (a point of catalogue 1) at a time;
-// anchors come from a global counter, in cell order.
+// One CTA of 256 threads owns one anchor (a point of catalogue 1) at a time.
+// Anchors come from a work queue whose positions name (batch item, anchor):
+// in cell order or in a learned order, taken from a shared counter (dynamic)
+// or as one contiguous range per CTA (static). A CTA keeps one histogram for
+// the item of its current anchor and adds it to that item's global histogram
+// when the item changes.
 //  Phase A  the 27 (cell, image) slots around the anchor's home cell are
 //           streamed from the cell list. A cell-local FP32 estimate of r1^2
 //           drops candidates certainly out of range; for the others the
@@ -44,8 +48,8 @@ constexpr unsigned kCodeExact = 0xFDu;
 #ifndef NCORR_ROW_UNROLL
 #define NCORR_ROW_UNROLL 2
 #endif
-constexpr int kSubJ = 32;                       // j-entries per work item
-constexpr int kSubPerTile = kTile / kSubJ;      // work items per tile pair
+// j-entries per work item: 8, 16 or 32 (a run-time choice, KArgs::sub_j).
+constexpr int kSubJDefault = 32;
 
 // Shared-memory layout (dynamic part). The bin table sits at offset 0 and the
 // CTA histogram right after it, so both are addressed with immediate offsets.
@@ -56,13 +60,13 @@ struct SmemLayout {
 __host__ __device__ inline int align16(int x) { return (x + 15) & ~15; }
 
 __host__ __device__ inline SmemLayout make_layout(int nb, int ks, bool sym, bool weighted,
-                                                  bool hist_global) {
+                                                  bool hist_global, int hist_copies = 1) {
   SmemLayout L;
   int o = 0;
   L.table = o;
   o += kTableSize;
   L.hist = o;
-  if (!hist_global) o = align16(o + nb * nb * nb * (weighted ? 8 : 4));
+  if (!hist_global) o = align16(o + hist_copies * nb * nb * nb * (weighted ? 8 : 4));
   L.e2 = o;
   o += ks * 16;
   L.e3 = sym ? L.e2 : o;
@@ -92,11 +96,24 @@ __host__ __device__ inline SmemLayout make_layout(int nb, int ks, bool sym, bool
 
 struct KArgs {
   Geom g;
-  Catalog c1, c2, c3;
+  const BatchItem* items;  // device array of n_items
+  int n_items;
+  // Work queue: position w stands for anchor q_anchor[w] (sorted index in
+  // catalogue 1) of item q_item[w]; null arrays mean item 0 and anchor w.
+  const int* q_item;
+  const int* q_anchor;
+  int n_work;
+  // 1: CTA b takes positions [b*n/G, (b+1)*n/G) in order (static schedule);
+  // 0: CTAs take positions from the shared counter `work`.
+  int sched_static;
+  int sub_j;        // j-entries per work item (8, 16 or 32)
+  int hist_copies;  // copies of the CTA histogram, lane & (copies-1) picks one
+  // Optional: candidate pairs of each anchor added to its home cell
+  // (cell_base of the item + cell), the work the scheduler learns.
+  unsigned long long* cell_work;
   const unsigned char* table;
   int* work;
   int* flags;
-  HistOut hist;
   // Per-CTA overflow slabs, two lists of kg entries each.
   float4* slab_e;
   unsigned* slab_m;
@@ -314,12 +331,12 @@ __device__ __forceinline__ unsigned lds_u32(unsigned addr) {
 // Histogram update. The key is the table-scaled code: a byte offset into the
 // shared histogram, or a plain bin index for the global histogram (HG).
 template <bool WEIGHTED, bool HG>
-__device__ __forceinline__ void hist_add(unsigned char* hist_s, const KArgs& a, unsigned key, float w) {
+__device__ __forceinline__ void hist_add(unsigned char* hist_s, const HistOut& hist, unsigned key, float w) {
   if (HG) {
     if (WEIGHTED)
-      add128(&a.hist.wsum[2 * key], __float2ll_rn(w));
+      add128(&hist.wsum[2 * key], __float2ll_rn(w));
     else
-      atomicAdd(&a.hist.counts[key], 1ull);
+      atomicAdd(&hist.counts[key], 1ull);
   } else {
     if (WEIGHTED)
       atomicAdd(reinterpret_cast<unsigned long long*>(hist_s + key),
@@ -339,8 +356,10 @@ __device__ __forceinline__ void settle_exact(const KArgs& a, const ExactEntry& e
   const int nb = g.nb;
   const int sj = static_cast<int>(e.meta & 31u), sl = static_cast<int>((e.meta >> 5) & 31u);
   const unsigned bj = (e.meta >> 10) & 0xffu, bl = (e.meta >> 18) & 0xffu;
-  const double4_16a pa = a.c1.pd[e.ai];
-  const int hc = a.c1.pc[e.ai];
+  const BatchItem& it = a.items[a.q_item ? a.q_item[e.ai] : 0];
+  const int ai = a.q_anchor ? a.q_anchor[e.ai] : e.ai;
+  const double4_16a pa = it.c1.pd[ai];
+  const int hc = it.c1.pc[ai];
   const int h[3] = {hc / (g.nc[2] * g.nc[1]), (hc / g.nc[2]) % g.nc[1], hc % g.nc[2]};
   double shj[3], shl[3];
   // Image shift of a slot (source/device.cu:89-122); zero in survey mode.
@@ -355,8 +374,8 @@ __device__ __forceinline__ void settle_exact(const KArgs& a, const ExactEntry& e
       if (cl == g.nc[d]) shl[d] = g.box[d]; else if (cl == -1) shl[d] = -g.box[d];
     }
   }
-  const double4_16a dj = a.c2.pd[e.pj];
-  const double4_16a dl = a.c3.pd[e.pl];
+  const double4_16a dj = it.c2.pd[e.pj];
+  const double4_16a dl = it.c3.pd[e.pl];
   const double jx = __dadd_rn(dj.x, shj[0]), jy = __dadd_rn(dj.y, shj[1]), jz = __dadd_rn(dj.z, shj[2]);
   const double lx = __dadd_rn(dl.x, shl[0]), ly = __dadd_rn(dl.y, shl[1]), lz = __dadd_rn(dl.z, shl[2]);
   const double r1 = sqr_sep_exact(pa.x, pa.y, pa.z, jx, jy, jz, g.fma_pattern);
@@ -371,9 +390,9 @@ __device__ __forceinline__ void settle_exact(const KArgs& a, const ExactEntry& e
   const unsigned key = (bj * nb + bl) * nb + static_cast<unsigned>(lo);
   if (WEIGHTED) {
     const float w = (static_cast<float>(pa.w) * static_cast<float>(dj.w)) * static_cast<float>(dl.w) * a.wscale;
-    add128(&a.hist.wsum[2 * key], __float2ll_rn(w));
+    add128(&it.hist.wsum[2 * key], __float2ll_rn(w));
   } else {
-    atomicAdd(&a.hist.counts[key], 1ull);
+    atomicAdd(&it.hist.counts[key], 1ull);
   }
 }
 
@@ -389,9 +408,10 @@ struct Cold {
   const float* e2hi;
   const double* sqr_bins;
   unsigned char* tab;
-  unsigned char* hist_s;
+  unsigned char* hist_s;  // this lane's copy of the CTA histogram
+  HistOut hist;           // the current item's global histogram
   int qn, xn;
-  int nb, cs, ai;
+  int nb, cs, ai;  // ai: the anchor's position in the work queue
   float wa;
   unsigned lane, lt_mask;
   unsigned long long n_exact_tri, n_queued, n_flag_rows;
@@ -455,7 +475,7 @@ __device__ __noinline__ void cold_drain(Cold& c) {
         xe.meta = (mj >> 8) | ((ml >> 8) << 5) | ((mj & 0xffu) << 10) | ((ml & 0xffu) << 18);
       } else if (code < static_cast<unsigned>(nb)) {
         const float wprod = WEIGHTED ? (c.wa * c.l2.W(j, a.ks)) * c.l3.W(l, a.ks) * a.wscale : 0.0f;
-        hist_add<WEIGHTED, HG>(c.hist_s, a, (key_jl + code) * c.cs, wprod);
+        hist_add<WEIGHTED, HG>(c.hist_s, c.hist, (key_jl + code) * c.cs, wprod);
       }
     }
     const unsigned xbal = __ballot_sync(0xffffffffu, exact);
@@ -527,18 +547,26 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
   __shared__ int s_start2[27], s_start3[27], s_pre2[28], s_pre3[28];
   __shared__ float s_do[27][3];
   __shared__ double s_shift[27][3];
-  __shared__ int s_anchor, s_k2, s_k3, s_item;
+  __shared__ int s_w, s_k2, s_k3, s_item, s_cur, s_sym6;
+  __shared__ long long s_next, s_end;
   __shared__ unsigned long long s_since;
+  __shared__ BatchItem s_it;  // the item of the current anchor
 
   const Geom& g = a.g;
   const int nb = g.nb;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const unsigned FULL = 0xffffffffu;
   const unsigned lt_mask = (1u << lane) - 1u;
-  const SmemLayout L = make_layout(nb, a.ks, SYM, WEIGHTED, HG);
+  const SmemLayout L = make_layout(nb, a.ks, SYM, WEIGHTED, HG, a.hist_copies);
   unsigned char* tab = smem + L.table;
   unsigned char* hist_s = smem + L.hist;
   const int nbin = nb * nb * nb;
+  const int copies = HG ? 1 : a.hist_copies;
+  // This lane's copy of the CTA histogram: lanes that hit one bin in the same
+  // instruction spread over the copies.
+  const unsigned copy_off = static_cast<unsigned>((lane & (copies - 1)) * nbin * (WEIGHTED ? 8 : 4));
+  const int sub_j = a.sub_j;
+  const int spt = kTile / sub_j;  // work items per tile pair
   const int cs = a.code_scale;
   const unsigned nb_cs = static_cast<unsigned>(nb * cs);
 
@@ -572,14 +600,20 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
   }
   for (int i = tid; i < g.tab_n; i += kThreads) tab[i] = a.table[i];
   if (!HG) {
-    for (int i = tid; i < nbin; i += kThreads) {
+    for (int i = tid; i < nbin * copies; i += kThreads) {
       if (WEIGHTED)
         reinterpret_cast<long long*>(hist_s)[i] = 0;
       else
         reinterpret_cast<unsigned*>(hist_s)[i] = 0;
     }
   }
-  if (tid == 0) s_since = 0;
+  if (tid == 0) {
+    s_since = 0;
+    s_cur = -1;
+    const long long n = a.n_work, G = gridDim.x, b = blockIdx.x;
+    s_next = b * n / G;
+    s_end = (b + 1) * n / G;
+  }
 
   Cold c;
   c.a = a.self;
@@ -591,7 +625,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
   c.e2hi = s_e2hi;
   c.sqr_bins = s_sqr_bins;
   c.tab = tab;
-  c.hist_s = hist_s;
+  c.hist_s = hist_s + copy_off;
+  c.hist.counts = nullptr;
+  c.hist.wsum = nullptr;
   c.qn = 0;
   c.xn = 0;
   c.nb = nb;
@@ -606,22 +642,25 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
 
   unsigned long long n_exact_pair = 0, n_anchor = 0, n_pairs = 0, n_evals = 0;
 
+  // Adds the CTA histogram (all copies) into the current item's histogram.
   auto flush = [&]() {
     for (int i = tid; i < (HG ? 0 : nbin); i += kThreads) {
       if (WEIGHTED) {
         long long* h = reinterpret_cast<long long*>(hist_s);
-        const long long v = h[i];
-        if (v) {
-          add128(&a.hist.wsum[2 * i], v);
-          h[i] = 0;
+        long long v = 0;
+        for (int cp = 0; cp < copies; ++cp) {
+          v += h[cp * nbin + i];
+          h[cp * nbin + i] = 0;
         }
+        if (v) add128(&s_it.hist.wsum[2 * i], v);
       } else {
         unsigned* h = reinterpret_cast<unsigned*>(hist_s);
-        const unsigned v = h[i];
-        if (v) {
-          atomicAdd(&a.hist.counts[i], static_cast<unsigned long long>(v));
-          h[i] = 0;
+        unsigned long long v = 0;
+        for (int cp = 0; cp < copies; ++cp) {
+          v += h[cp * nbin + i];
+          h[cp * nbin + i] = 0;
         }
+        if (v) atomicAdd(&s_it.hist.counts[i], v);
       }
     }
   };
@@ -630,20 +669,40 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
   const unsigned tab_sh = static_cast<unsigned>(__cvta_generic_to_shared(tab));
   const unsigned tab_adj = tab_sh - 0x4B000000u;
   const unsigned tab_last = tab_sh + static_cast<unsigned>(g.tab_n - 1);
-  const unsigned hist_sh = static_cast<unsigned>(__cvta_generic_to_shared(hist_s));
+  const unsigned hist_sh = static_cast<unsigned>(__cvta_generic_to_shared(hist_s)) + copy_off;
   const unsigned dummy = static_cast<unsigned>(__cvta_generic_to_shared(smem + L.scratch)) + 4u * lane;
   const float tscale = g.tab_scale, ha = g.ha, hb = g.hb;
 
   for (;;) {
     __syncthreads();
-    if (tid == 0) s_anchor = atomicAdd(a.work, 1);
+    if (tid == 0) {
+      if (a.sched_static)
+        s_w = s_next < s_end ? static_cast<int>(s_next++) : a.n_work;
+      else
+        s_w = atomicAdd(a.work, 1);
+    }
     __syncthreads();
-    const int ai = s_anchor;
-    if (ai >= a.c1.n) break;
+    const int w = s_w;
+    if (static_cast<unsigned>(w) >= static_cast<unsigned>(a.n_work)) break;
+    const int item = a.q_item ? a.q_item[w] : 0;
+    if (item != s_cur) {
+      // New item: its predecessor's counts go to the predecessor's histogram.
+      if (s_cur >= 0) flush();
+      __syncthreads();
+      if (tid == 0) {
+        s_it = a.items[item];
+        s_sym6 = item_sym6(a.items[item]) ? 1 : 0;
+        s_cur = item;
+        s_since = 0;
+      }
+      __syncthreads();
+    }
+    c.hist = s_it.hist;
+    const int ai = a.q_anchor ? a.q_anchor[w] : w;
     ++n_anchor;
-    const double4_16a pa = a.c1.pd[ai];
-    const float4 qa = a.c1.pq[ai];
-    const int hc = a.c1.pc[ai];
+    const double4_16a pa = s_it.c1.pd[ai];
+    const float4 qa = s_it.c1.pq[ai];
+    const int hc = s_it.c1.pc[ai];
     const int hz = hc % g.nc[2];
     const int hy = (hc / g.nc[2]) % g.nc[1];
     const int hx = hc / (g.nc[2] * g.nc[1]);
@@ -679,11 +738,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
           s_do[s][d] = 0.0f;
         }
       }
-      s_start2[s] = ok ? a.c2.start[cell] : 0;
-      s_pre2[s + 1] = ok ? a.c2.count[cell] : 0;
+      s_start2[s] = ok ? s_it.c2.start[cell] : 0;
+      s_pre2[s + 1] = ok ? s_it.c2.count[cell] : 0;
       if (!SYM) {
-        s_start3[s] = ok ? a.c3.start[cell] : 0;
-        s_pre3[s + 1] = ok ? a.c3.count[cell] : 0;
+        s_start3[s] = ok ? s_it.c3.start[cell] : 0;
+        s_pre3[s + 1] = ok ? s_it.c3.count[cell] : 0;
       }
     }
     __syncthreads();
@@ -700,7 +759,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
     __syncthreads();
 
     // ---- Phase A: neighbour lists
-    const bool after_only = SYM && a.sym6;
+    const bool after_only = SYM && s_sym6;
     auto build = [&](const Catalog& cat, const int* pre, const int* st, ListView& lv, int* counter) {
       const int total = pre[27];
       const int rounded = (total + 31) & ~31;
@@ -775,15 +834,17 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
         }
       }
     };
-    build(a.c2, s_pre2, s_start2, l2, &s_k2);
-    if (!SYM) build(a.c3, s_pre3, s_start3, l3, &s_k3);
+    build(s_it.c2, s_pre2, s_start2, l2, &s_k2);
+    if (!SYM) build(s_it.c3, s_pre3, s_start3, l3, &s_k3);
     __syncthreads();
     const int cap = a.ks + a.kg;
     const int k2 = min(s_k2, cap);
     const int k3 = SYM ? k2 : min(s_k3, cap);
     if (tid == 0) {
-      n_pairs += SYM ? static_cast<unsigned long long>(k2) * (k2 > 0 ? k2 - 1 : 0) / 2
-                     : static_cast<unsigned long long>(k2) * k3;
+      const unsigned long long pairs_here = SYM ? static_cast<unsigned long long>(k2) * (k2 > 0 ? k2 - 1 : 0) / 2
+                                                : static_cast<unsigned long long>(k2) * k3;
+      n_pairs += pairs_here;
+      if (a.cell_work) atomicAdd(&a.cell_work[s_it.cell_base + hc], pairs_here);
       n_evals += static_cast<unsigned long long>(s_pre2[27]) +
                  (SYM ? 0ull : static_cast<unsigned long long>(s_pre3[27]));
     }
@@ -791,13 +852,13 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
     const int nt3 = (k3 + kTile - 1) / kTile;
     const long long npairs_t = SYM ? static_cast<long long>(nt2) * (nt2 + 1) / 2
                                    : static_cast<long long>(nt2) * nt3;
-    const long long nitems = npairs_t * kSubPerTile;
-    // A CTA histogram bin grows by at most kSubJ*kTile per item; flush before
+    const long long nitems = npairs_t * spt;
+    // A CTA histogram bin grows by at most sub_j*kTile per item; flush before
     // it could overflow its 32-bit counter (count mode) or 64-bit sum
     // (weighted mode, |term| <= 2^30).
-    const long long kItemLimit = (1LL << 31) / (static_cast<long long>(kSubJ) * kTile);
+    const long long kItemLimit = (1LL << 31) / (static_cast<long long>(sub_j) * kTile);
     const float wa = static_cast<float>(pa.w);
-    c.ai = ai;
+    c.ai = w;
     c.wa = wa;
 
     for (long long m0 = 0; m0 < nitems; m0 += kItemLimit) {
@@ -836,14 +897,15 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
             wl[r] = 0.0f;
           }
         }
-        const int jb = jt * kTile + sub * kSubJ;
-        const int je = min(jb + kSubJ, k2);
+        const int jb = jt * kTile + sub * sub_j;
+        const int je = min(jb + sub_j, k2);
         const bool j_in_smem = jb < a.ks;
         const float4* ej_base = j_in_smem ? l2.e + jb : l2.se + (jb - a.ks);
         const unsigned* mj_base = j_in_smem ? l2.m + jb : l2.sm + (jb - a.ks);
         const float* wj_base = WEIGHTED ? (j_in_smem ? l2.w + jb : l2.sw + (jb - a.ks)) : nullptr;
         const unsigned kj_mul = static_cast<unsigned>(nb * nb * cs);
-        const int rmin = DIAG ? sub : 0;  // l-slices r < sub lie entirely below these rows
+        // l-slices r < rmin lie entirely below these rows.
+        const int rmin = DIAG ? (sub * sub_j) >> 5 : 0;
         // Rows with a candidate needing the careful/exact path are flagged
         // here and re-examined out of line after the loop.
         unsigned rowmask = 0;
@@ -931,7 +993,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
               }
               const unsigned key = kj + kl[r] + code;
               if (HG) {
-                if (ok && clean) hist_add<WEIGHTED, true>(hist_s, a, key, wja * wl[r]);
+                if (ok && clean) hist_add<WEIGHTED, true>(hist_s, c.hist, key, wja * wl[r]);
               } else {
                 red_shared_u64_if(key, static_cast<unsigned long long>(__float2ll_rn(wja * wl[r])), ok && clean);
               }
@@ -954,8 +1016,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
         mi = __shfl_sync(FULL, mi, 0);
         const long long m = m0 + mi;
         if (m >= m1) break;
-        const int sub = static_cast<int>(m % kSubPerTile);
-        const long long tp = m / kSubPerTile;
+        const int sub = static_cast<int>(m % spt);
+        const long long tp = m / spt;
         int jt, lt;
         if (SYM) {
           lt = static_cast<int>((sqrtf(8.0f * static_cast<float>(tp) + 1.0f) - 1.0f) * 0.5f);
@@ -966,7 +1028,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
           jt = static_cast<int>(tp % nt2);
           lt = static_cast<int>(tp / nt2);
         }
-        if (jt * kTile + sub * kSubJ >= k2) continue;  // empty sub-range of the last tile
+        if (jt * kTile + sub * sub_j >= k2) continue;  // empty sub-range of the last tile
         if (SYM && jt == lt)
           item(jt, lt, sub, std::true_type());
         else
@@ -979,7 +1041,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
   }
   cold_flush_exact<SURVEY, WEIGHTED>(c);
   __syncthreads();
-  flush();
+  if (s_cur >= 0) flush();
   if (a.stats) {
     atomicAdd(&a.stats[0], c.n_exact_tri);
     atomicAdd(&a.stats[1], n_exact_pair);

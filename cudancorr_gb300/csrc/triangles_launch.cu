@@ -3,12 +3,15 @@
 
 namespace ncorr_gb300 {
 
+// set_attr false: the shared-memory attribute was set by an earlier launch
+// (inside a stream capture only kernel nodes are recorded).
 template <bool SV, bool SYM, bool W, bool HG>
-static cudaError_t launch_one(const KArgs& a, int grid, size_t smem, cudaStream_t st) {
-  cudaError_t e = cudaFuncSetAttribute(k_triangles<SV, SYM, W, HG>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       static_cast<int>(smem));
-  if (e != cudaSuccess) return e;
+static cudaError_t launch_one(const KArgs& a, int grid, size_t smem, cudaStream_t st, bool set_attr) {
+  if (set_attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_triangles<SV, SYM, W, HG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem));
+    if (e != cudaSuccess) return e;
+  }
   k_triangles<SV, SYM, W, HG><<<grid, kThreads, smem, st>>>(a);
   return cudaGetLastError();
 }
@@ -30,8 +33,9 @@ static int occupancy_one(size_t smem) {
 }
 
 template <bool SV, bool SYM, bool W>
-static cudaError_t launch_hg(const KArgs& a, bool hg, int grid, size_t smem, cudaStream_t st) {
-  return hg ? launch_one<SV, SYM, W, true>(a, grid, smem, st) : launch_one<SV, SYM, W, false>(a, grid, smem, st);
+static cudaError_t launch_hg(const KArgs& a, bool hg, int grid, size_t smem, cudaStream_t st, bool set_attr) {
+  return hg ? launch_one<SV, SYM, W, true>(a, grid, smem, st, set_attr)
+            : launch_one<SV, SYM, W, false>(a, grid, smem, st, set_attr);
 }
 
 template <bool SV, bool SYM, bool W>
@@ -40,17 +44,18 @@ static int occupancy_hg(bool hg, size_t smem) {
 }
 
 cudaError_t launch_triangles(const KArgs& a, bool survey, bool sym, bool weighted, bool hg, int grid,
-                             size_t smem, cudaStream_t st) {
+                             size_t smem, cudaStream_t st, bool set_attr) {
+  const bool s = set_attr;
   if (survey) {
-    if (sym) return weighted ? launch_hg<true, true, true>(a, hg, grid, smem, st)
-                             : launch_hg<true, true, false>(a, hg, grid, smem, st);
-    return weighted ? launch_hg<true, false, true>(a, hg, grid, smem, st)
-                    : launch_hg<true, false, false>(a, hg, grid, smem, st);
+    if (sym) return weighted ? launch_hg<true, true, true>(a, hg, grid, smem, st, s)
+                             : launch_hg<true, true, false>(a, hg, grid, smem, st, s);
+    return weighted ? launch_hg<true, false, true>(a, hg, grid, smem, st, s)
+                    : launch_hg<true, false, false>(a, hg, grid, smem, st, s);
   }
-  if (sym) return weighted ? launch_hg<false, true, true>(a, hg, grid, smem, st)
-                           : launch_hg<false, true, false>(a, hg, grid, smem, st);
-  return weighted ? launch_hg<false, false, true>(a, hg, grid, smem, st)
-                  : launch_hg<false, false, false>(a, hg, grid, smem, st);
+  if (sym) return weighted ? launch_hg<false, true, true>(a, hg, grid, smem, st, s)
+                           : launch_hg<false, true, false>(a, hg, grid, smem, st, s);
+  return weighted ? launch_hg<false, false, true>(a, hg, grid, smem, st, s)
+                  : launch_hg<false, false, false>(a, hg, grid, smem, st, s);
 }
 
 int triangles_occupancy(bool survey, bool sym, bool weighted, bool hg, size_t smem) {
@@ -79,20 +84,20 @@ void launch_exact(const KArgs& a, bool survey, bool weighted, int grid, cudaStre
   }
 }
 
-// Folds the unsorted (bin_j, bin_l, bin_3) histogram into the reference's
-// triCountsAll_ layout: out[hi + mid*nb + lo*nb^2] for lo <= mid <= hi sums
-// the distinct permutations in a fixed order (deterministic), times `factor`
-// (2 when only pairs j < l were visited, 6 when only i < j < l).
-__global__ void k_fold(const unsigned long long* __restrict__ counts,
-                       const unsigned long long* __restrict__ wsum, int nb, int weighted,
-                       double factor, double inv_scale, double* __restrict__ out,
-                       unsigned long long* __restrict__ total) {
+// Folds each item's unsorted (bin_j, bin_l, bin_3) histogram into the
+// reference's triCountsAll_ layout: out[hi + mid*nb + lo*nb^2] for
+// lo <= mid <= hi sums the distinct permutations in a fixed order
+// (deterministic), times 2 when only pairs j < l were visited (p2 == p3) or 6
+// when only i < j < l were. blockIdx.y is the item.
+__global__ void k_fold(const BatchItem* __restrict__ items, int nb, int weighted, int sym, double inv_scale) {
+  const BatchItem& it = items[blockIdx.y];
   const int nbin = nb * nb * nb;
-  int f = blockIdx.x * blockDim.x + threadIdx.x;
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= nbin) return;
-  int hi = f % nb, mid = (f / nb) % nb, lo = f / (nb * nb);
+  const double factor = item_sym6(it) ? 6.0 : (sym ? 2.0 : 1.0);
+  const int hi = f % nb, mid = (f / nb) % nb, lo = f / (nb * nb);
   if (!(lo <= mid && mid <= hi)) {
-    out[f] = 0.0;
+    it.out[f] = 0.0;
     return;
   }
   const int v[3] = {lo, mid, hi};
@@ -102,7 +107,7 @@ __global__ void k_fold(const unsigned long long* __restrict__ counts,
   double acc = 0.0;
   unsigned long long cnt = 0;
   for (int p = 0; p < 6; ++p) {
-    int key = (v[perm[p][0]] * nb + v[perm[p][1]]) * nb + v[perm[p][2]];
+    const int key = (v[perm[p][0]] * nb + v[perm[p][1]]) * nb + v[perm[p][2]];
     bool dup = false;
     for (int q = 0; q < ns; ++q) dup = dup || (seen[q] == key);
     if (dup) continue;
@@ -110,34 +115,33 @@ __global__ void k_fold(const unsigned long long* __restrict__ counts,
     if (weighted) {
       // Signed 128-bit (hi, lo) to double: negate negative values in integer
       // arithmetic first, so the conversion never cancels.
-      unsigned long long lo = wsum[2 * key];
-      unsigned long long hi = wsum[2 * key + 1];
-      const bool neg = static_cast<long long>(hi) < 0;
+      unsigned long long wl = it.hist.wsum[2 * key];
+      unsigned long long wh = it.hist.wsum[2 * key + 1];
+      const bool neg = static_cast<long long>(wh) < 0;
       if (neg) {
-        lo = ~lo + 1ull;
-        hi = ~hi + (lo == 0ull ? 1ull : 0ull);
+        wl = ~wl + 1ull;
+        wh = ~wh + (wl == 0ull ? 1ull : 0ull);
       }
-      const double mag = static_cast<double>(hi) * 18446744073709551616.0 + static_cast<double>(lo);
+      const double mag = static_cast<double>(wh) * 18446744073709551616.0 + static_cast<double>(wl);
       acc += (neg ? -mag : mag) * inv_scale;
     } else {
-      cnt += counts[key];
+      cnt += it.hist.counts[key];
     }
   }
   if (weighted) {
-    out[f] = acc * factor;
+    it.out[f] = acc * factor;
   } else {
-    unsigned long long c = cnt * static_cast<unsigned long long>(factor);
-    out[f] = static_cast<double>(c);
-    if (c) atomicAdd(total, c);
+    const unsigned long long c = cnt * static_cast<unsigned long long>(factor);
+    it.out[f] = static_cast<double>(c);
+    if (c) atomicAdd(it.total, c);
   }
 }
 
-void launch_fold(const unsigned long long* counts, const unsigned long long* wsum, int nb,
-                 bool weighted, double factor, double inv_scale, double* out,
-                 unsigned long long* total, cudaStream_t st) {
-  int nbin = nb * nb * nb;
-  k_fold<<<(nbin + 255) / 256, 256, 0, st>>>(counts, wsum, nb, weighted ? 1 : 0, factor, inv_scale,
-                                             out, total);
+void launch_fold(const BatchItem* items, int n_items, int nb, bool weighted, bool sym, double inv_scale,
+                 cudaStream_t st) {
+  const int nbin = nb * nb * nb;
+  const dim3 grid((nbin + 255) / 256, n_items);
+  k_fold<<<grid, 256, 0, st>>>(items, nb, weighted ? 1 : 0, sym ? 1 : 0, inv_scale);
 }
 
 }  // namespace ncorr_gb300

@@ -170,6 +170,97 @@ int ncorr_count_noalloc(const double box[3], const double* edges, int n_edges, i
                         const double* d_p1, int64_t n1, const double* d_p2, int64_t n2,
                         const double* d_p3, int64_t n3, double* d_counts_all, void* stream);
 
+/* ---- Work-queue scheduling. No counterpart in the reference, whose kernel
+ * gives one thread to each anchor in input order (source/device.cu:259-315).
+ * The schedule changes only the order in which CTAs take anchors; the counts
+ * never depend on it. */
+enum { NCORR_SCHED_DYNAMIC = 0, NCORR_SCHED_STATIC = 1, NCORR_SCHED_LEARNED = 2 };
+
+/* The scheduler's work model: an MLP 28 -> 64 -> 64 -> 1 (ReLU) that maps a
+ * cell's occupancies (log(1 + n) of its catalogue-1 count and of the 27
+ * neighbour-slot counts) to log(1 + candidate pairs of its anchors). */
+typedef struct ncorr_sched ncorr_sched;
+
+/* Anchor order of later calls on h. DYNAMIC (default): cells in grid order,
+ * CTAs take anchors from a shared counter. STATIC: cells in grid order, each
+ * CTA one contiguous range. LEARNED: cells ordered by the work `model`
+ * predicts, heaviest first, taken from a shared counter. `model` must stay
+ * alive while h uses it. */
+int ncorr_set_schedule(ncorr_handle* h, int mode, const ncorr_sched* model);
+
+/* Tuning of later calls: j-entries per work item (8, 16 or 32) and copies of
+ * each CTA histogram (1, 2 or 4). The results do not depend on them. */
+int ncorr_set_tuning(ncorr_handle* h, int sub_j, int hist_copies);
+
+/* When on, later calls record for each cell of the grid its 28 scheduler
+ * features and the candidate pairs its catalogue-1 anchors took: the
+ * training data of the work model. */
+int ncorr_set_record_work(ncorr_handle* h, int on);
+int64_t ncorr_num_cells(const ncorr_handle* h);
+/* feats: n_cells x 28 floats; work: n_cells doubles (either may be null). */
+int ncorr_get_cell_work(const ncorr_handle* h, float* feats, double* work, int64_t cap_cells);
+
+/* Model life cycle; parameters are initialised from `seed` (He-uniform
+ * weights, zero biases) on the current device. */
+int ncorr_sched_create(uint64_t seed, ncorr_sched** out);
+void ncorr_sched_destroy(ncorr_sched* s);
+int ncorr_sched_num_params(void);
+/* Parameter vector: W1 [28][64], b1 [64], W2 [64][64], b2 [64], w3 [64], b3. */
+int ncorr_sched_get_params(const ncorr_sched* s, float* out, int64_t cap);
+int ncorr_sched_set_params(ncorr_sched* s, const float* in, int64_t n);
+/* out[i] = model(feats[i]) for n host rows of 28 floats. */
+int ncorr_sched_predict(ncorr_sched* s, const float* feats, int64_t n, float* out);
+/* Gradient of the mean squared error (1/n) sum (model(x_i) - t_i)^2 over n
+ * host samples, by the training kernels; *loss = sum of squared errors. */
+int ncorr_sched_gradient(ncorr_sched* s, const float* feats, const float* target, int64_t n, float* grad,
+                         float* loss);
+/* Adam training on the GPU: `epochs` passes over the n samples in minibatches
+ * of `batch` (a multiple of 64), shuffled from `seed`; *last_epoch_loss = mean
+ * squared error over the last epoch. */
+int ncorr_sched_train(ncorr_sched* s, const float* feats, const float* target, int64_t n, int epochs, int batch,
+                      float lr, uint64_t seed, float* last_epoch_loss);
+
+/* ---- Batches: many catalogue triples counted by one persistent launch of
+ * the triangle kernel, captured with everything around it (copies, cell
+ * lists, queue, exact pass, fold) in one CUDA graph. No counterpart in the
+ * reference, where each triple is a separate calculateD1D2D3. All items share
+ * h's box and bins; in every item either p2 == p3 or p2 != p3 (same array
+ * and size), uniformly. Arrays (host, or device when on_device) are bound to
+ * the batch: each ncorr_batch_run counts their current contents. */
+typedef struct ncorr_batch ncorr_batch;
+
+typedef struct ncorr_batch_stats {
+  double ms_plan;       /* host wall time of ncorr_batch_create */
+  double ms_autotune;   /* part of it spent timing tuning candidates */
+  double ms_run;        /* device time of the last ncorr_batch_run graph */
+  double ms_count;      /* device time of its triangle kernel */
+  uint64_t n_work;      /* anchors in the queue (all items) */
+  uint64_t n_pairs;     /* candidate triangles of the last run */
+  uint64_t n_pair_evals; /* candidate neighbours scanned in the last run */
+  uint64_t triangles;   /* sum over items of the folded counts (count mode) */
+  int n_items;
+  int n_catalogues;     /* distinct arrays gridded */
+  int sub_j;            /* tuning in use */
+  int hist_copies;
+  int grid_ctas;
+  int weighted;
+  int graph_nodes;
+} ncorr_batch_stats;
+
+/* Plans the batch: grids and checks every catalogue once, sizes the lists,
+ * builds the queue with h's schedule, times the tuning candidates on a
+ * sample of the queue when `autotune` (else uses h's tuning), and captures
+ * the graph. */
+int ncorr_batch_create(ncorr_handle* h, int n_items, const double* const* p1, const int64_t* n1,
+                       const double* const* p2, const int64_t* n2, const double* const* p3, const int64_t* n3,
+                       int on_device, int autotune, ncorr_batch** out);
+/* Replays the graph on `stream` (null: the batch's own) and waits for it. */
+int ncorr_batch_run(ncorr_batch* b, void* stream);
+/* triCountsAll_ of item `item` after the last run (nb^3 doubles). */
+int ncorr_batch_get_counts_all(const ncorr_batch* b, int item, double* out, int64_t cap);
+int ncorr_batch_get_stats(const ncorr_batch* b, ncorr_batch_stats* out);
+void ncorr_batch_destroy(ncorr_batch* b);
+
 #ifdef __cplusplus
 }
 #endif
