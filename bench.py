@@ -471,6 +471,153 @@ def run_batch(args) -> dict:
     return out if rank == 0 else None
 
 
+SURVEY_COMBOS = (("DDD", 4), ("DDR", 32), ("DRR", 64), ("RRR", 256))  # (triple, anchor sampling 1/f)
+
+
+def survey_catalogues(seed: int):
+    """Data 500k (lognormal(0, 0.3) weights) and randoms 2.5M in the RA 0-90,
+    Dec 0-60 wedge, r ~ N(1000, 150) in [600, 1400], jointly shifted by the
+    engine's prep_cat_survey; 15 log bins in [5, 120)."""
+    from cudancorr_gb300 import api
+    from cudancorr_gb300 import catalogs as C
+    d = C.survey_wedge(500_000, seed, True)
+    r = C.survey_wedge(2_500_000, seed + 1, False)
+    box, ori = api.prep_cat_survey(d, r)
+    return d, r, box, ori, api.logspace(5.0, 120.0, 16)
+
+
+def run_survey(args) -> dict:
+    """Survey mode with weights: DDD, DDR, DRR and RRR per step, each on a
+    seeded anchor sample (fractions in SURVEY_COMBOS); weighted bins checked
+    per bin against the FP64 oracle on a few anchors."""
+    import torch
+    from cudancorr_gb300 import api
+    from oracle import oracle as O
+
+    world, rank, local = dist_setup()
+    d, r, box, ori, edges = survey_catalogues(7 + 10 * rank)
+    dev = torch.device("cuda", local)
+    cats = {"D": d, "R": r}
+    tcat = {k: torch.from_numpy(v).to(dev) for k, v in cats.items()}
+    rng = np.random.default_rng(3)
+    runs = []
+    triples = args.triples.split(",") if args.triples else [c for c, _ in SURVEY_COMBOS]
+    for combo, frac in SURVEY_COMBOS:
+        if combo not in triples:
+            continue
+        frac *= args.anchor_scale
+        anc = cats[combo[0]]
+        sub = np.ascontiguousarray(anc[np.sort(rng.choice(len(anc), len(anc) // frac, replace=False))])
+        runs.append((combo, frac, sub, torch.from_numpy(sub).to(dev)))
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    corr = api.ncorr(box, api.threeD, edges, True, ori)
+
+    def call(t1, combo):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        corr._calculate_device(t1, tcat[combo[1]], tcat[combo[2]], stream=stream.cuda_stream)
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1), corr.stats()
+
+    # Triangles of each sample: the same call with unit weights (the
+    # geometry, not the weights, decides which triangles count).
+    ones = {k: v.clone() for k, v in tcat.items()}
+    for v in ones.values():
+        v[:, 3] = 1.0
+    tri = {}
+    for combo, frac, sub, tsub in runs:
+        t1 = tsub.clone()
+        t1[:, 3] = 1.0
+        corr._calculate_device(t1, ones[combo[1]], ones[combo[2]], stream=stream.cuda_stream)
+        tri[combo] = corr.stats()["triangles"]
+    del ones
+
+    for _ in range(args.warmup):
+        for combo, frac, sub, tsub in runs[:1]:
+            call(tsub, combo)
+    sampler = ClockSampler(local)
+    sampler.start()
+    barrier(world)
+    step_ms, kernel_ms, per = [], [], {c: [] for c, _, _, _ in runs}
+    flops = []
+    for _ in range(args.steps):
+        tot = 0.0
+        for combo, frac, sub, tsub in runs:
+            ms, st = call(tsub, combo)
+            tot += ms
+            per[combo].append(ms)
+            kernel_ms.append(st["ms_count"])
+            flops.append(8.0 * (st["n_pairs"] + st["n_pair_evals"]))
+        step_ms.append(tot)
+    barrier(world)
+    clocks = sampler.stop()
+    total_ms = barrier_max(sum(step_ms), world)
+    tri_step = float(sum(tri.values()))
+
+    # End to end: host arrays through the reference-facing call.
+    e2e_ms = []
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for combo, frac, sub, tsub in runs:
+            corr.calculateD1D2D3(sub, cats[combo[1]], cats[combo[2]])
+            _ = corr.getTriCountsOut()
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    e2e_total = barrier_max(sum(e2e_ms), world)
+
+    # Precision: weighted bins against the FP64 oracle on a few anchors.
+    precision = {}
+    for combo, n_anc in (("DDD", 32), ("DDR", 8), ("DRR", 8)) if not args.no_cpu_baseline else ():
+        sub = np.ascontiguousarray(cats[combo[0]][:n_anc])
+        corr.calculateD1D2D3(sub, cats[combo[1]], cats[combo[2]])
+        h = corr.getTriCountsAll()
+        ref = O.count_threeD(box, edges, sub, cats[combo[1]], cats[combo[2]], survey=True,
+                             nthreads=os.cpu_count() or 1)
+        nz = ref != 0
+        rel = np.abs(h[nz] - ref[nz]) / np.abs(ref[nz])
+        precision[combo] = {"anchors": n_anc, "bins": int(nz.sum()), "max_rel_err": float(rel.max()),
+                            "median_rel_err": float(np.median(rel)),
+                            "nonzero_pattern_equal": bool(np.array_equal(h != 0, nz))}
+    corr.close()
+
+    sm_mhz = clocks.get("sm_mhz") or 1995.0
+    peak_tflops = N_SM * FP32_LANES_PER_SM * 2 * sm_mhz * 1e6 / 1e12
+    achieved = sum(flops) / (sum(kernel_ms) / 1e3) / 1e12
+    nb = len(edges) - 1
+    out = {
+        "metric": METRIC, "value": barrier_sum(tri_step * args.steps, world) / (total_ms / 1e3), "unit": UNIT,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32+fp64-exact, int128 sums",
+        "data": "synthetic (seeded)",
+        "config": {"workload": "survey", "description": "survey wedge: data 500,000 (lognormal(0,0.3) weights), "
+                                                       "randoms 2,500,000, 15 log bins in [5,120), weighted "
+                                                       "DDD/DDR/DRR/RRR, anchors sampled per triple",
+                   "anchor_fraction": {c: f"1/{f}" for c, f, _, _ in runs}, "box": [float(x) for x in box],
+                   "bins_per_side": nb, "triangles_per_step": int(tri_step),
+                   "triangles_per_triple": {c: int(v) for c, v in tri.items()},
+                   "l2": "flushed (256 MiB write) before every call", "parallelism": "independent catalogues per GPU"},
+        "e2e": {"value": barrier_sum(tri_step * args.steps, world) / (e2e_total / 1e3), "unit": UNIT,
+                "h2d_bytes_per_step": int(sum(sub.nbytes + cats[c[1]].nbytes + (0 if c[2] == c[1] else cats[c[2]].nbytes)
+                                              for c, _, sub, _ in runs)),
+                "d2h_bytes_per_step": int(len(runs) * nb ** 3 * 8), "ms_per_step": e2e_total / args.steps},
+        "roofline": {"bound": "fp32_issue", "achieved": achieved, "peak": peak_tflops, "unit": "TFLOP/s",
+                     "frac": achieved / peak_tflops, "traffic": None, "kernel": "k_triangles",
+                     "kernel_ms": sum(kernel_ms) / args.steps,
+                     "work": "8 flops x (candidate triangles W + pair-stage evaluations P), four calls",
+                     "peak_basis": "152 SMs x 128 FP32 lanes x 2 x median sampled SM clock"},
+        "gpu_launches": 6 * len(runs) * args.steps,
+        "clocks": clocks,
+        "per_triple_ms": {c: statistics.mean(v) for c, v in per.items()},
+        "precision_vs_fp64_oracle": precision,
+    }
+    return out if rank == 0 else None
+
+
 def run_reference(args) -> dict:
     """The reference's own kernel (oracle/_ref cubin, compiled unmodified from
     its source/device.cu) behind a restatement of its host flow, on a random
@@ -492,9 +639,9 @@ def run_reference(args) -> dict:
         O.runner()
     except Exception as e:  # the cubin is built where the reference sources are mounted
         return {"impl": "reference", "unavailable": f"reference kernel not loadable: {e}"}
-    if args.workload == "batch_mocks":
-        return {"impl": "reference", "unavailable": "the reference arm times the single-catalogue workloads; "
-                                                    "batch_mocks would be 64 reference calls of hours each"}
+    if args.workload in ("batch_mocks", "survey"):
+        return {"impl": "reference", "unavailable": "the reference arm times the single-catalogue box workloads; "
+                                                    f"{args.workload} would take the reference kernel hours"}
     p, box, edges, desc = workload(args.workload, 0)
     from cudancorr_gb300 import catalogs as C
     wp, wbox, wedges = C.config_box_uniform()
@@ -538,10 +685,13 @@ def main():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--workload", default="box_clustered",
                     choices=["box_clustered", "box_clustered_L1000", "box_uniform", "soneira_peebles",
-                             "batch_mocks"])
+                             "batch_mocks", "survey"])
     ap.add_argument("--schedule", default="dynamic", choices=["dynamic", "static", "learned"],
                     help="anchor order of the triangle kernel (learned: trains the work model first)")
     ap.add_argument("--no-autotune", action="store_true", help="batch_mocks: default tuning")
+    ap.add_argument("--triples", default="", help="survey: comma-separated subset of DDD,DDR,DRR,RRR")
+    ap.add_argument("--anchor-scale", type=int, default=1,
+                    help="survey: divide each triple's anchor sample by this factor (profiling size)")
     ap.add_argument("--ref-anchors", type=int, default=152 * 4 * 64)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--anchor-slab", type=float, default=None,
@@ -551,6 +701,8 @@ def main():
         out = run_reference(args)
     elif args.workload == "batch_mocks":
         out = run_batch(args)
+    elif args.workload == "survey":
+        out = run_survey(args)
     else:
         out = run_engine(args)
     if out is not None:

@@ -88,8 +88,8 @@ __host__ __device__ inline SmemLayout make_layout(int nb, int ks, bool sym, bool
   o += kWarps * kQueueCap * 8;
   L.xbuf = o;  // per warp: 32 uncertain candidates awaiting the exact kernel
   o += kWarps * 32 * 16;
-  L.scratch = o;  // one word per lane: sink of non-counting reductions
-  o += 32 * 4;
+  L.scratch = o;  // 8 bytes per lane: sink of non-counting reductions
+  o += 32 * 8;
   L.total = align16(o);
   return L;
 }
@@ -299,6 +299,71 @@ __device__ __forceinline__ unsigned cand_count(float ex, float ey, float ez, flo
   return q;
 }
 
+// The weighted twin of cand_count: the same classification, then the
+// fixed-point weight w_row * w_l (|value| <= 2^30 by the choice of the scale,
+// so the 32-bit conversion is exact and equals the 64-bit one) added into the
+// int64 bin, or into the lane's 8-byte scratch word when it does not count.
+// A 64-bit shared-memory add is not a native atomic (it compiles to a
+// compare-and-swap loop), so the add is split over the bin's two 32-bit
+// words with native atomics: the low word by atom.add, whose old value gives
+// the carry, then the high word by the sign extension plus that carry. Every
+// thread's carry comes from its own atomic on the low word, so the 64-bit
+// total is exact however the adds interleave.
+template <bool DIAG>
+__device__ __forceinline__ unsigned cand_wsum(float ex, float ey, float ez, float a, float a4, float lx,
+                                              float ly, float lz, float b, unsigned kj, unsigned kl,
+                                              unsigned in, float tscale, unsigned tab_adj, unsigned tab_last,
+                                              unsigned nb_cs, float ha, float hb, unsigned dummy, float wrow,
+                                              float wl) {
+  unsigned q;
+#define NCORR_CAND_WSUM_ASM                                                                           \
+  asm volatile(                                                                                      \
+      "{\n\t" NCORR_CAND_DECLS                                                                        \
+      ".reg .f32 wp;\n\t.reg .b32 wi, whi, wold, wnew, wcy, adrh;\n\t" NCORR_CAND_CLASSIFY              \
+      "add.u32 key, %10, %11;\n\t"                                                                   \
+      "add.u32 key, key, code;\n\t"                                                                  \
+      "selp.b32 adr, key, %19, upd;\n\t"                                                             \
+      "mul.rn.f32 wp, %20, %21;\n\t"                                                                 \
+      "cvt.rni.s32.f32 wi, wp;\n\t"                                                                  \
+      "shr.s32 whi, wi, 31;\n\t"                                                                     \
+      "atom.shared.add.u32 wold, [adr], wi;\n\t"                                                     \
+      "add.u32 wnew, wold, wi;\n\t"                                                                  \
+      "set.lt.u32.u32 wcy, wnew, wold;\n\t"                                                          \
+      "sub.u32 whi, whi, wcy;\n\t"                                                                   \
+      "add.u32 adrh, adr, 4;\n\t"                                                                    \
+      "red.shared.add.u32 [adrh], whi;\n\t"                                                          \
+      "}"                                                                                            \
+      : "=r"(q)                                                                                      \
+      : "f"(ex), "f"(ey), "f"(ez), "f"(a), "f"(a4), "f"(lx), "f"(ly), "f"(lz), "f"(b), "r"(kj), "r"(kl), \
+        "r"(in), "f"(tscale), "r"(tab_adj), "r"(tab_last), "r"(nb_cs), "f"(ha), "f"(hb), "r"(dummy),   \
+        "f"(wrow), "f"(wl))
+  if (DIAG) {
+#define NCORR_CAND_MASK NCORR_CAND_MASK_ON
+    NCORR_CAND_WSUM_ASM;
+#undef NCORR_CAND_MASK
+  } else {
+#define NCORR_CAND_MASK ""
+    NCORR_CAND_WSUM_ASM;
+#undef NCORR_CAND_MASK
+  }
+#undef NCORR_CAND_WSUM_ASM
+  return q;
+}
+
+// Counting body of the shared-histogram path: count or weighted sum.
+template <bool WEIGHTED, bool DIAG>
+__device__ __forceinline__ unsigned cand_body(float ex, float ey, float ez, float a, float a4, float lx,
+                                              float ly, float lz, float b, unsigned kj, unsigned kl,
+                                              unsigned in, float tscale, unsigned tab_adj, unsigned tab_last,
+                                              unsigned nb_cs, float ha, float hb, unsigned dummy, float wrow,
+                                              float wl) {
+  if (WEIGHTED)
+    return cand_wsum<DIAG>(ex, ey, ez, a, a4, lx, ly, lz, b, kj, kl, in, tscale, tab_adj, tab_last, nb_cs, ha, hb,
+                           dummy, wrow, wl);
+  return cand_count<DIAG>(ex, ey, ez, a, a4, lx, ly, lz, b, kj, kl, in, tscale, tab_adj, tab_last, nb_cs, ha, hb,
+                          dummy);
+}
+
 // The same classification without the histogram update: 1 when the
 // candidate needs the careful/exact path.
 __device__ __forceinline__ unsigned cand_flag(float ex, float ey, float ez, float a, float a4, float lx,
@@ -314,6 +379,12 @@ __device__ __forceinline__ unsigned cand_flag(float ex, float ey, float ez, floa
         "r"(in), "f"(tscale), "r"(tab_adj), "r"(tab_last), "r"(nb_cs), "f"(ha), "f"(hb));
 #undef NCORR_CAND_MASK
   return q;
+}
+
+__device__ __forceinline__ float lds_f32(unsigned addr) {
+  float v;
+  asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(addr));
+  return v;
 }
 
 __device__ __forceinline__ float4 lds_f4(unsigned addr) {
@@ -670,7 +741,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
   const unsigned tab_adj = tab_sh - 0x4B000000u;
   const unsigned tab_last = tab_sh + static_cast<unsigned>(g.tab_n - 1);
   const unsigned hist_sh = static_cast<unsigned>(__cvta_generic_to_shared(hist_s)) + copy_off;
-  const unsigned dummy = static_cast<unsigned>(__cvta_generic_to_shared(smem + L.scratch)) + 4u * lane;
+  const unsigned dummy = static_cast<unsigned>(__cvta_generic_to_shared(smem + L.scratch)) + 8u * lane;
   const float tscale = g.tab_scale, ha = g.ha, hb = g.hb;
 
   for (;;) {
@@ -910,33 +981,37 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
         // here and re-examined out of line after the loop.
         unsigned rowmask = 0;
 
-        if (!WEIGHTED && !HG) {
-          // Unweighted, shared histogram: the PTX candidate body. The lane's
-          // four l-entries are explicit scalars; slices below the diagonal
-          // are skipped with a warp-uniform test.
+        if (!HG) {
+          // Shared histogram: the PTX candidate body, counts or weighted
+          // sums. The lane's four l-entries are explicit scalars; slices
+          // below the diagonal are skipped with a warp-uniform test. A row's
+          // weight is (w_anchor * w_j) * scale, the order of the exact path.
           const float4 L0 = el[0], L1 = el[1], L2 = el[2], L3 = el[3];
           const unsigned K0 = kl[0], K1 = kl[1], K2 = kl[2], K3 = kl[3];
+          const float W0 = wl[0], W1 = wl[1], W2 = wl[2], W3 = wl[3];
           const int lr0 = lb + lane, lr1 = lr0 + 32, lr2 = lr0 + 64, lr3 = lr0 + 96;
-          auto row = [&](float4 e, unsigned k, int jj) -> unsigned {
+          const float wsc = a.wscale;
+          auto row = [&](float4 e, unsigned k, int jj, float wr) -> unsigned {
             const float a4 = 4.0f * e.w;
             unsigned q = 0;
             if (!DIAG || rmin <= 0)
-              q |= cand_count<DIAG>(e.x, e.y, e.z, e.w, a4, L0.x, L0.y, L0.z, L0.w, k, K0, jj < lr0, tscale,
-                                    tab_adj, tab_last, nb_cs, ha, hb, dummy);
+              q |= cand_body<WEIGHTED, DIAG>(e.x, e.y, e.z, e.w, a4, L0.x, L0.y, L0.z, L0.w, k, K0, jj < lr0,
+                                             tscale, tab_adj, tab_last, nb_cs, ha, hb, dummy, wr, W0);
             if (!DIAG || rmin <= 1)
-              q |= cand_count<DIAG>(e.x, e.y, e.z, e.w, a4, L1.x, L1.y, L1.z, L1.w, k, K1, jj < lr1, tscale,
-                                    tab_adj, tab_last, nb_cs, ha, hb, dummy);
+              q |= cand_body<WEIGHTED, DIAG>(e.x, e.y, e.z, e.w, a4, L1.x, L1.y, L1.z, L1.w, k, K1, jj < lr1,
+                                             tscale, tab_adj, tab_last, nb_cs, ha, hb, dummy, wr, W1);
             if (!DIAG || rmin <= 2)
-              q |= cand_count<DIAG>(e.x, e.y, e.z, e.w, a4, L2.x, L2.y, L2.z, L2.w, k, K2, jj < lr2, tscale,
-                                    tab_adj, tab_last, nb_cs, ha, hb, dummy);
-            q |= cand_count<DIAG>(e.x, e.y, e.z, e.w, a4, L3.x, L3.y, L3.z, L3.w, k, K3, jj < lr3, tscale,
-                                  tab_adj, tab_last, nb_cs, ha, hb, dummy);
+              q |= cand_body<WEIGHTED, DIAG>(e.x, e.y, e.z, e.w, a4, L2.x, L2.y, L2.z, L2.w, k, K2, jj < lr2,
+                                             tscale, tab_adj, tab_last, nb_cs, ha, hb, dummy, wr, W2);
+            q |= cand_body<WEIGHTED, DIAG>(e.x, e.y, e.z, e.w, a4, L3.x, L3.y, L3.z, L3.w, k, K3, jj < lr3,
+                                           tscale, tab_adj, tab_last, nb_cs, ha, hb, dummy, wr, W3);
             return __any_sync(FULL, q != 0) ? 1u : 0u;
           };
           int j = jb;
           if (j_in_smem) {
             const unsigned e_sh = static_cast<unsigned>(__cvta_generic_to_shared(l2.e + jb));
             const unsigned m_sh = static_cast<unsigned>(__cvta_generic_to_shared(l2.m + jb));
+            const unsigned w_sh = WEIGHTED ? static_cast<unsigned>(__cvta_generic_to_shared(l2.w + jb)) : 0u;
 #if NCORR_ROW_UNROLL == 2
             for (; j + 1 < je; j += 2) {
               const unsigned o = static_cast<unsigned>(j - jb);
@@ -944,8 +1019,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
               const float4 e1 = lds_f4(e_sh + 16u * o + 16u);
               const unsigned k0 = (lds_u32(m_sh + 4u * o) & 0xffu) * kj_mul + hist_sh;
               const unsigned k1 = (lds_u32(m_sh + 4u * o + 4u) & 0xffu) * kj_mul + hist_sh;
-              const unsigned f0 = row(e0, k0, j);
-              const unsigned f1 = row(e1, k1, j + 1);
+              const float w0 = WEIGHTED ? wa * lds_f32(w_sh + 4u * o) * wsc : 0.0f;
+              const float w1 = WEIGHTED ? wa * lds_f32(w_sh + 4u * o + 4u) * wsc : 0.0f;
+              const unsigned f0 = row(e0, k0, j, w0);
+              const unsigned f1 = row(e1, k1, j + 1, w1);
               rowmask |= (f0 | (f1 << 1)) << o;
             }
 #endif
@@ -953,16 +1030,19 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
               const unsigned o = static_cast<unsigned>(j - jb);
               const float4 e0 = lds_f4(e_sh + 16u * o);
               const unsigned k0 = (lds_u32(m_sh + 4u * o) & 0xffu) * kj_mul + hist_sh;
-              rowmask |= row(e0, k0, j) << o;
+              const float w0 = WEIGHTED ? wa * lds_f32(w_sh + 4u * o) * wsc : 0.0f;
+              rowmask |= row(e0, k0, j, w0) << o;
             }
           } else {
             for (; j < je; ++j) {
               const unsigned o = static_cast<unsigned>(j - jb);
-              rowmask |= row(ej_base[o], (mj_base[o] & 0xffu) * kj_mul + hist_sh, j) << o;
+              const float w0 = WEIGHTED ? wa * wj_base[o] * wsc : 0.0f;
+              rowmask |= row(ej_base[o], (mj_base[o] & 0xffu) * kj_mul + hist_sh, j, w0) << o;
             }
           }
         } else {
-          // Weighted sums or global histogram: the same decisions in C++.
+          // Global histogram (too many bins for shared memory): the same
+          // decisions in C++.
           for (int j = jb; j < je; ++j) {
             const unsigned o = static_cast<unsigned>(j - jb);
             const float4 ej = ej_base[o];
