@@ -28,7 +28,7 @@
 //           (bin_j, bin_l, bin_3) histogram. Candidates whose FP32
 //           classification is not certain are queued per warp and settled by
 //           the exact FP64 restatement.
-// Symmetry: with catalogues 2 and 3 identical (SYM), only pairs j < l are
+// Symmetry: with catalogues 2 and 3 identical (SYM), only pairs l < j are
 // visited and count twice -- the reference's ordered double loop is symmetric
 // in (p2, p3) because (a-b)^2 == (b-a)^2 bit for bit. With all three
 // catalogues identical and the geometry checked to make every triangle's
@@ -214,7 +214,7 @@ __device__ __forceinline__ void red_shared_u64_if(unsigned addr, unsigned long l
 // flag "needs the careful/exact path". Every rounding is explicit (.rn),
 // matching the error model. kj/kl are byte offsets into the shared histogram
 // (kj includes its base address); `in` masks the candidate (diagonal tiles:
-// j < l). The reduction is unconditional: a candidate that does not count
+// l < j). The reduction is unconditional: a candidate that does not count
 // adds to the lane's own scratch word `dummy` instead, which keeps the loop
 // free of the branch a predicated atomic compiles to.
 // Classification of one candidate, shared verbatim by the counting body and
@@ -265,7 +265,7 @@ __device__ __forceinline__ void red_shared_u64_if(unsigned addr, unsigned long l
 // flag "needs the careful/exact path". Every rounding is explicit (.rn),
 // matching the error model. kj/kl are byte offsets into the shared histogram
 // (kj includes its base address); `in` masks the candidate (diagonal tiles:
-// j < l). The reduction is unconditional: a candidate that does not count
+// l < j). The reduction is unconditional: a candidate that does not count
 // adds to the lane's own scratch word `dummy` instead, which keeps the loop
 // free of the branch a predicated atomic compiles to.
 template <bool DIAG>
@@ -562,20 +562,21 @@ __device__ __noinline__ void cold_drain(Cold& c) {
 // Re-examines row j of a work item (lane's l-entries el[r] at lb + 32r + lane)
 // and queues the candidates that need the careful/exact path, with the same
 // decisions the counting body took. Inline: it only recomputes flags.
-template <bool WEIGHTED, bool HG, bool DIAG>
+template <bool WEIGHTED, bool HG, int MODE>
 __device__ __forceinline__ void enqueue_row(Cold& c, const Geom& g, int j, float4 ej, const float4 (&el)[kReg],
-                                            int lb, int rmin, unsigned tab_adj, unsigned tab_last,
+                                            int lb, int rhi, unsigned tab_adj, unsigned tab_last,
                                             unsigned nb_cs) {
+  constexpr bool DIAG = MODE == 2;
   const float a4 = 4.0f * ej.w;
   ++c.n_flag_rows;
 #pragma unroll
   for (int r = 0; r < kReg; ++r) {
     const int lr = lb + r * 32 + static_cast<int>(c.lane);
     bool want = false;
-    if (!DIAG || r >= rmin) {
+    if (MODE == 0 || r < rhi) {
       if (!WEIGHTED && !HG) {
         want = cand_flag(ej.x, ej.y, ej.z, ej.w, a4, el[r].x, el[r].y, el[r].z, el[r].w,
-                         DIAG ? static_cast<unsigned>(j < lr) : 1u, g.tab_scale, tab_adj, tab_last, nb_cs, g.ha,
+                         DIAG ? static_cast<unsigned>(j > lr) : 1u, g.tab_scale, tab_adj, tab_last, nb_cs, g.ha,
                          g.hb) != 0;
       } else {
         const float dx = ej.x - el[r].x;
@@ -590,7 +591,7 @@ __device__ __forceinline__ void enqueue_row(Cold& c, const Geom& g, int j, float
         const float S = s + v;
         const bool clean = H > S * fmaf(g.ha, S, g.hb);
         want = code == kCodeCareful || (code < nb_cs && !clean);
-        if (DIAG) want = want && (j < lr);
+        if (DIAG) want = want && (j > lr);
       }
     }
     const unsigned bal = __ballot_sync(0xffffffffu, want);
@@ -947,8 +948,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
       __syncthreads();
 
       // One work item: l-tile lt (registers) against 32 j-entries of tile jt.
-      auto item = [&](int jt, int lt, int sub, auto diag_tag) {
-        constexpr bool DIAG = decltype(diag_tag)::value;
+      // MODE 0: full l-tile; 1: the list's partial last l-tile; 2: diagonal
+      // tile pair (identical catalogues, pairs j > l only).
+      auto item = [&](int jt, int lt, int sub, auto mode_tag) {
+        constexpr int MODE = decltype(mode_tag)::value;
+        constexpr bool DIAG = MODE == 2;
         float4 el[kReg];
         unsigned kl[kReg];
         float wl[kReg];
@@ -975,8 +979,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
         const unsigned* mj_base = j_in_smem ? l2.m + jb : l2.sm + (jb - a.ks);
         const float* wj_base = WEIGHTED ? (j_in_smem ? l2.w + jb : l2.sw + (jb - a.ks)) : nullptr;
         const unsigned kj_mul = static_cast<unsigned>(nb * nb * cs);
-        // l-slices r < rmin lie entirely below these rows.
-        const int rmin = DIAG ? (sub * sub_j) >> 5 : 0;
+        // l-slices r >= rhi hold no candidate of these rows: they lie past
+        // the end of the list or, on the diagonal, at or above the rows.
+        const int rhi = MODE == 0 ? kReg : min(kReg, (min(k3, DIAG ? je : k3) - lb + 31) >> 5);
         // Rows with a candidate needing the careful/exact path are flagged
         // here and re-examined out of line after the loop.
         unsigned rowmask = 0;
@@ -984,7 +989,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
         if (!HG) {
           // Shared histogram: the PTX candidate body, counts or weighted
           // sums. The lane's four l-entries are explicit scalars; slices
-          // below the diagonal are skipped with a warp-uniform test. A row's
+          // without candidates are skipped with a warp-uniform test. A row's
           // weight is (w_anchor * w_j) * scale, the order of the exact path.
           const float4 L0 = el[0], L1 = el[1], L2 = el[2], L3 = el[3];
           const unsigned K0 = kl[0], K1 = kl[1], K2 = kl[2], K3 = kl[3];
@@ -994,17 +999,17 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
           auto row = [&](float4 e, unsigned k, int jj, float wr) -> unsigned {
             const float a4 = 4.0f * e.w;
             unsigned q = 0;
-            if (!DIAG || rmin <= 0)
-              q |= cand_body<WEIGHTED, DIAG>(e.x, e.y, e.z, e.w, a4, L0.x, L0.y, L0.z, L0.w, k, K0, jj < lr0,
-                                             tscale, tab_adj, tab_last, nb_cs, ha, hb, dummy, wr, W0);
-            if (!DIAG || rmin <= 1)
-              q |= cand_body<WEIGHTED, DIAG>(e.x, e.y, e.z, e.w, a4, L1.x, L1.y, L1.z, L1.w, k, K1, jj < lr1,
+            q |= cand_body<WEIGHTED, DIAG>(e.x, e.y, e.z, e.w, a4, L0.x, L0.y, L0.z, L0.w, k, K0, jj > lr0,
+                                           tscale, tab_adj, tab_last, nb_cs, ha, hb, dummy, wr, W0);
+            if (MODE == 0 || rhi > 1)
+              q |= cand_body<WEIGHTED, DIAG>(e.x, e.y, e.z, e.w, a4, L1.x, L1.y, L1.z, L1.w, k, K1, jj > lr1,
                                              tscale, tab_adj, tab_last, nb_cs, ha, hb, dummy, wr, W1);
-            if (!DIAG || rmin <= 2)
-              q |= cand_body<WEIGHTED, DIAG>(e.x, e.y, e.z, e.w, a4, L2.x, L2.y, L2.z, L2.w, k, K2, jj < lr2,
+            if (MODE == 0 || rhi > 2)
+              q |= cand_body<WEIGHTED, DIAG>(e.x, e.y, e.z, e.w, a4, L2.x, L2.y, L2.z, L2.w, k, K2, jj > lr2,
                                              tscale, tab_adj, tab_last, nb_cs, ha, hb, dummy, wr, W2);
-            q |= cand_body<WEIGHTED, DIAG>(e.x, e.y, e.z, e.w, a4, L3.x, L3.y, L3.z, L3.w, k, K3, jj < lr3,
-                                           tscale, tab_adj, tab_last, nb_cs, ha, hb, dummy, wr, W3);
+            if (MODE == 0 || rhi > 3)
+              q |= cand_body<WEIGHTED, DIAG>(e.x, e.y, e.z, e.w, a4, L3.x, L3.y, L3.z, L3.w, k, K3, jj > lr3,
+                                             tscale, tab_adj, tab_last, nb_cs, ha, hb, dummy, wr, W3);
             return __any_sync(FULL, q != 0) ? 1u : 0u;
           };
           int j = jb;
@@ -1052,7 +1057,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
             bool q = false;
 #pragma unroll
             for (int r = 0; r < kReg; ++r) {
-              if (DIAG && r < rmin) continue;
+              if (MODE != 0 && r >= rhi) continue;
               const float dx = ej.x - el[r].x;
               const float dy = ej.y - el[r].y;
               const float dz = ej.z - el[r].z;
@@ -1067,7 +1072,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
               bool ok = code < nb_cs;
               bool careful = code == kCodeCareful;
               if (DIAG) {
-                const bool in = j < lb + r * 32 + lane;
+                const bool in = j > lb + r * 32 + lane;
                 ok = ok && in;
                 careful = careful && in;
               }
@@ -1086,7 +1091,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
           const int bit = __ffs(rowmask) - 1;
           rowmask &= rowmask - 1u;
           if (c.qn > kQueueCap - kTile) cold_drain<SURVEY, WEIGHTED, HG>(c);
-          enqueue_row<WEIGHTED, HG, DIAG>(c, g, jb + bit, ej_base[bit], el, lb, rmin, tab_adj, tab_last, nb_cs);
+          enqueue_row<WEIGHTED, HG, MODE>(c, g, jb + bit, ej_base[bit], el, lb, rhi, tab_adj, tab_last, nb_cs);
         }
       };
 
@@ -1100,19 +1105,23 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
         const long long tp = m / spt;
         int jt, lt;
         if (SYM) {
-          lt = static_cast<int>((sqrtf(8.0f * static_cast<float>(tp) + 1.0f) - 1.0f) * 0.5f);
-          while (static_cast<long long>(lt) * (lt + 1) / 2 > tp) --lt;
-          while (static_cast<long long>(lt + 1) * (lt + 2) / 2 <= tp) ++lt;
-          jt = static_cast<int>(tp - static_cast<long long>(lt) * (lt + 1) / 2);
+          // Tile pairs lt <= jt: the list's partial last tile is a j-tile
+          // (rows stop at the list end) except on its own diagonal.
+          jt = static_cast<int>((sqrtf(8.0f * static_cast<float>(tp) + 1.0f) - 1.0f) * 0.5f);
+          while (static_cast<long long>(jt) * (jt + 1) / 2 > tp) --jt;
+          while (static_cast<long long>(jt + 1) * (jt + 2) / 2 <= tp) ++jt;
+          lt = static_cast<int>(tp - static_cast<long long>(jt) * (jt + 1) / 2);
         } else {
           jt = static_cast<int>(tp % nt2);
           lt = static_cast<int>(tp / nt2);
         }
         if (jt * kTile + sub * sub_j >= k2) continue;  // empty sub-range of the last tile
         if (SYM && jt == lt)
-          item(jt, lt, sub, std::true_type());
+          item(jt, lt, sub, std::integral_constant<int, 2>());
+        else if ((lt + 1) * kTile > k3)
+          item(jt, lt, sub, std::integral_constant<int, 1>());
         else
-          item(jt, lt, sub, std::false_type());
+          item(jt, lt, sub, std::integral_constant<int, 0>());
       }
       // Queue entries refer to this anchor's lists: settle them now.
       if (c.qn > 0) cold_drain<SURVEY, WEIGHTED, HG>(c);
