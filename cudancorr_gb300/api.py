@@ -4,6 +4,7 @@ The reference's public surface is a C++ class (include/cudaNcorr.hpp:10-68 of
 cudaNcorr); this module keeps its names and argument meaning:
 
     corr = ncorr(box, 0, bins, isSurvey, ori)      # ncorr::ncorr (threeD)
+    corr = ncorr(box, 1, bins, numMinorBins, isSurvey, ori)   # (rppi)
     corr.calculateD1D2D3(p1, p2, p3)               # N x 4 (x, y, z, w) arrays
     corr.getTriBinsOut(); corr.getTriCountsOut(); corr.getPiBinsOut()
 
@@ -36,10 +37,12 @@ threeD, rppi, smu = 0, 1, 2  # ncorr::binType (include/cudaNcorr.hpp:12)
 # Every symbol the C header declares (include/ncorr_gb300.h).
 EXPORTS = (
     "ncorr_create", "ncorr_create_rppi", "ncorr_destroy", "ncorr_calculate_d1d2d3",
-    "ncorr_calculate_d1d2d3_device", "ncorr_num_out", "ncorr_num_bins", "ncorr_get_tri_bins_out",
+    "ncorr_calculate_d1d2d3_device", "ncorr_num_out", "ncorr_num_bins", "ncorr_num_pi_bins",
+    "ncorr_get_tri_bins_out",
     "ncorr_get_pi_bins_out", "ncorr_get_tri_counts_out", "ncorr_get_tri_counts_all",
     "ncorr_get_stats", "ncorr_last_error", "survey_prep_cat", "survey_prep_cat2",
     "survey_convert_coordinates", "ncorr_logspace", "ncorr_count_noalloc",
+    "ncorr_write_three_d", "ncorr_write_rppi", "ncorr_read_catalog_txt", "ncorr_random_catalog",
     "ncorr_set_schedule", "ncorr_set_tuning", "ncorr_set_record_work", "ncorr_num_cells",
     "ncorr_get_cell_work", "ncorr_sched_create", "ncorr_sched_destroy", "ncorr_sched_num_params",
     "ncorr_sched_get_params", "ncorr_sched_set_params", "ncorr_sched_predict", "ncorr_sched_gradient",
@@ -67,7 +70,7 @@ class NcorrStats(ctypes.Structure):
         ("n_exact_pairs", ctypes.c_uint64), ("n_exact_tris", ctypes.c_uint64),
         ("triangles", ctypes.c_uint64), ("n_flagged_rows", ctypes.c_uint64), ("n_queued", ctypes.c_uint64),
         ("weighted", ctypes.c_int), ("symmetric", ctypes.c_int),
-        ("grid_ctas", ctypes.c_int), ("list_capacity", ctypes.c_int),
+        ("grid_ctas", ctypes.c_int), ("list_capacity", ctypes.c_int), ("overflow", ctypes.c_double),
     ]
 
     def as_dict(self) -> dict:
@@ -120,6 +123,7 @@ def load_library() -> ctypes.CDLL:
         "ncorr_calculate_d1d2d3_device": (i32, [vp, vp, i64, vp, i64, vp, i64, vp]),
         "ncorr_num_out": (i64, [vp]),
         "ncorr_num_bins": (i32, [vp]),
+        "ncorr_num_pi_bins": (i32, [vp]),
         "ncorr_get_tri_bins_out": (i32, [vp, _D, i64]),
         "ncorr_get_pi_bins_out": (i32, [vp, _D, i64, ctypes.POINTER(i64)]),
         "ncorr_get_tri_counts_out": (i32, [vp, _D, i64]),
@@ -130,6 +134,10 @@ def load_library() -> ctypes.CDLL:
         "survey_prep_cat2": (i32, [_D, i64, _D, i64, _D, _D]),
         "survey_convert_coordinates": (i32, [_D, _D, i64, _D]),
         "ncorr_logspace": (i32, [ctypes.c_double, ctypes.c_double, i32, _D]),
+        "ncorr_write_three_d": (i32, [ctypes.c_char_p, _D, _D, i64]),
+        "ncorr_write_rppi": (i32, [ctypes.c_char_p, _D, _D, _D, i64]),
+        "ncorr_read_catalog_txt": (i32, [ctypes.c_char_p, _D, ctypes.POINTER(i32), _D, i64, ctypes.POINTER(i64)]),
+        "ncorr_random_catalog": (i32, [i64, _D, ctypes.c_uint64, _D]),
         "ncorr_count_noalloc": (i32, [_D, _D, i32, i32, vp, i64, vp, i64, vp, i64, vp, vp]),
         "ncorr_set_schedule": (i32, [vp, i32, vp]),
         "ncorr_set_tuning": (i32, [vp, i32, i32]),
@@ -184,10 +192,27 @@ def as_catalog(p) -> np.ndarray:
 
 
 class ncorr:
-    """threeD (r1, r2, r3) triangle counter, the reference's `ncorr` class."""
+    """Triangle counter, the reference's `ncorr` class: threeD (r1, r2, r3)
+    bins with ncorr(box, 0, bins, isSurvey, ori), or rppi (rp bins of all
+    three sides, unit pi bins of the two shortest) with
+    ncorr(box, 1, bins, numMinorBins, isSurvey, ori) (numMinorBins may also
+    be given by keyword)."""
 
-    def __init__(self, box, bin_type, bins, isSurvey=False, ori=(0.0, 0.0, 0.0),
-                 numMinorBins: Optional[int] = None):
+    def __init__(self, box, bin_type, bins, *args, isSurvey=None, ori=None, numMinorBins: Optional[int] = None):
+        # The reference's two constructors (include/cudaNcorr.hpp:14-15):
+        #   (box, bin_type, bins, isSurvey, ori)
+        #   (box, bin_type, bins, numMinorBins, isSurvey, ori)
+        if len(args) == 3:
+            numMinorBins, isSurvey, ori = args
+        elif len(args) <= 2:
+            if len(args) >= 1:
+                isSurvey = args[0]
+            if len(args) == 2:
+                ori = args[1]
+        else:
+            raise TypeError("ncorr(box, bin_type, bins, [numMinorBins,] isSurvey, ori)")
+        isSurvey = False if isSurvey is None else isSurvey
+        ori = (0.0, 0.0, 0.0) if ori is None else ori
         lib = load_library()
         self._h = ctypes.c_void_p()
         self._box = _vec3(box)
@@ -224,6 +249,16 @@ class ncorr:
     @property
     def num_bins(self) -> int:
         return int(self._lib.ncorr_num_bins(self._h))
+
+    @property
+    def num_pi_bins(self) -> int:
+        """numPiBins_ (rppi); 0 for threeD."""
+        return int(self._lib.ncorr_num_pi_bins(self._h))
+
+    @property
+    def num_counts_all(self) -> int:
+        npi = self.num_pi_bins
+        return self.num_bins ** 3 * (npi * npi if npi else 1)
 
     def calculateD1D2D3(self, p1, p2, p3) -> None:
         """Counts triangles with p1 as anchors (source/cudaNcorr.cu:220-430).
@@ -266,11 +301,17 @@ class ncorr:
         return out
 
     def getPiBinsOut(self) -> np.ndarray:
-        """Always empty for the threeD bin type (source/cudaNcorr.cu:110-112)."""
+        """(n_out, 2) pi bins (l, m) for rppi; empty for threeD (source/cudaNcorr.cu:110-112)."""
         n = ctypes.c_int64(0)
         buf = np.zeros(1, dtype=np.float64)
-        _check(self._lib.ncorr_get_pi_bins_out(self._h, _dptr(buf), 0, ctypes.byref(n)))
-        return np.zeros((n.value, 2), dtype=np.float64)
+        _check(self._lib.ncorr_get_pi_bins_out(self._h, _dptr(buf), 0, ctypes.byref(n))
+               if self.num_pi_bins == 0 else NCORR_OK)
+        if self.num_pi_bins == 0:
+            return np.zeros((n.value, 2), dtype=np.float64)
+        m = int(self._lib.ncorr_num_out(self._h))
+        out = np.zeros((m, 2), dtype=np.float64)
+        _check(self._lib.ncorr_get_pi_bins_out(self._h, _dptr(out), out.size, ctypes.byref(n)))
+        return out
 
     def getTriCountsOut(self) -> np.ndarray:
         """Compacted counts of the last calculation (source/cudaNcorr.cu:114-116)."""
@@ -280,9 +321,9 @@ class ncorr:
         return out
 
     def getTriCountsAll(self) -> np.ndarray:
-        """Full nb^3 histogram (the reference's private triCountsAll_)."""
-        nb = self.num_bins
-        out = np.zeros(nb ** 3, dtype=np.float64)
+        """Full histogram (the reference's private triCountsAll_): nb^3
+        entries, or nb^3 * numPiBins^2 for rppi."""
+        out = np.zeros(self.num_counts_all, dtype=np.float64)
         _check(self._lib.ncorr_get_tri_counts_all(self._h, _dptr(out), out.size))
         return out
 
@@ -470,4 +511,44 @@ def logspace(start: float, end: float, n: int) -> np.ndarray:
     """logspace (source/utils.cu:16-27)."""
     out = np.zeros(n)
     _check(load_library().ncorr_logspace(float(start), float(end), int(n), _dptr(out)))
+    return out
+
+
+def writeToFileThreeD(filename, triBins, counts) -> None:
+    """writeToFileThreeD (source/utils.cu:161-181): rows "r1 r2 r3 count", 6 decimals."""
+    b = np.ascontiguousarray(np.asarray(triBins, dtype=np.float64).reshape(-1, 3))
+    c = np.ascontiguousarray(np.asarray(counts, dtype=np.float64).reshape(-1))
+    if b.shape[0] != c.shape[0]:
+        raise NcorrError(NCORR_ERR_INVALID_ARGUMENT, "Vectors have different sizes.")
+    _check(load_library().ncorr_write_three_d(str(filename).encode(), _dptr(b), _dptr(c), c.shape[0]))
+
+
+def writeToFileRppi(filename, triBins, piBins, counts) -> None:
+    """writeToFileRppi (source/utils.cu:183-208): rows "r1 r2 r3 pi1 pi2 count"."""
+    b = np.ascontiguousarray(np.asarray(triBins, dtype=np.float64).reshape(-1, 3))
+    p = np.ascontiguousarray(np.asarray(piBins, dtype=np.float64).reshape(-1, 2))
+    c = np.ascontiguousarray(np.asarray(counts, dtype=np.float64).reshape(-1))
+    if not (b.shape[0] == p.shape[0] == c.shape[0]):
+        raise NcorrError(NCORR_ERR_INVALID_ARGUMENT, "Vectors have different sizes.")
+    _check(load_library().ncorr_write_rppi(str(filename).encode(), _dptr(b), _dptr(p), _dptr(c), c.shape[0]))
+
+
+def readCatalogTxt(filename, box, pos_columns=(0, 1, 2, 3)) -> np.ndarray:
+    """readCatalogTxt (source/utils.cu:119-159): N x 4 (x, y, z, w) from text."""
+    lib = load_library()
+    b = _vec3(box)
+    cols = (ctypes.c_int * 4)(*[int(c) for c in pos_columns])
+    n = ctypes.c_int64(0)
+    _check(lib.ncorr_read_catalog_txt(str(filename).encode(), _dptr(b), cols, None, 0, ctypes.byref(n)))
+    out = np.zeros((n.value, 4), dtype=np.float64)
+    _check(lib.ncorr_read_catalog_txt(str(filename).encode(), _dptr(b), cols, _dptr(out), n.value, ctypes.byref(n)))
+    return out
+
+
+def generateRandomCatalog(Np: int, box, seed: int = 0) -> np.ndarray:
+    """generateRandomCatalog (source/utils.cu:41-52): Np points uniform in
+    [0, box), weight 1; seeded here (the reference seeds from the clock)."""
+    b = _vec3(box)
+    out = np.zeros((int(Np), 4), dtype=np.float64)
+    _check(load_library().ncorr_random_catalog(int(Np), _dptr(b), ctypes.c_uint64(seed), _dptr(out)))
     return out

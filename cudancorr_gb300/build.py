@@ -21,10 +21,12 @@ OUT = PKG / "lib"
 OBJ = PKG / "lib" / "obj"
 LIBNAME = "libcudancorr_gb300.so"
 
-SOURCES = ["cell_list.cu", "triangles_launch.cu", "sched.cu", "capi.cu", "sched_api.cu", "batch.cu"]
+SOURCES = ["cell_list.cu", "triangles_launch.cu", "sched.cu", "capi.cu", "sched_api.cu", "batch.cu", "rppi.cu", "utils.cu"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
-         "-Xptxas", "-warn-spills"]
+# Host code: no implicit FMA contraction, so that host arithmetic (bin
+# edges, tables, coordinates) gives the same bits on x86 and Arm hosts.
+FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+         "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
 
 
 def nvcc() -> str:

@@ -486,6 +486,8 @@ int ncorr_batch_create(ncorr_handle* h, int n_items, const double* const* p1, co
   if (!out) return fail(NCORR_ERR_INVALID_ARGUMENT, "null output pointer");
   *out = nullptr;
   if (!h) return fail(NCORR_ERR_INVALID_ARGUMENT, "null handle");
+  if (h->bin_type != NCORR_BIN_THREED)
+    return fail(NCORR_ERR_NOT_IMPLEMENTED, "batches are implemented for the threeD bin type");
   if (n_items < 1 || n_items > (1 << 20) || !p1 || !n1 || !p2 || !n2 || !p3 || !n3)
     return fail(NCORR_ERR_INVALID_ARGUMENT, "bad batch arrays");
   cudaGetLastError();

@@ -385,16 +385,56 @@ int ncorr_create(const double box[3], int bin_type, const double* edges, int n_e
 
 int ncorr_create_rppi(const double box[3], int bin_type, const double* edges, int n_edges,
                       int num_minor_bins, int is_survey, const double ori[3], ncorr_handle** out) {
-  (void)box;
-  (void)edges;
-  (void)n_edges;
-  (void)num_minor_bins;
-  (void)is_survey;
-  (void)ori;
-  if (out) *out = nullptr;
+  if (!out) return fail(NCORR_ERR_INVALID_ARGUMENT, "null handle pointer");
+  *out = nullptr;
   if (bin_type != NCORR_BIN_RPPI)
     return fail(NCORR_ERR_INVALID_ARGUMENT, "Invalid constructor call for bin_type.");
-  return fail(NCORR_ERR_NOT_IMPLEMENTED, "the rppi bin type is not implemented by this engine");
+  if (!box || !edges) return fail(NCORR_ERR_INVALID_ARGUMENT, "null box or edges");
+  if (n_edges < 2 || n_edges > kMaxEdges)
+    return fail(NCORR_ERR_INVALID_ARGUMENT, "need 2..128 bin edges");
+  for (int i = 0; i < n_edges; ++i)
+    if (!std::isfinite(edges[i])) return fail(NCORR_ERR_INVALID_ARGUMENT, "non-finite bin edge");
+  if (edges[0] < 0.0) return fail(NCORR_ERR_INVALID_ARGUMENT, "negative first bin edge");
+  for (int i = 1; i < n_edges; ++i)
+    if (!(edges[i] > edges[i - 1]) || !(edges[i] * edges[i] > edges[i - 1] * edges[i - 1]))
+      return fail(NCORR_ERR_INVALID_ARGUMENT, "bin edges must be strictly increasing");
+  // The reference builds piBins_ = 0, 1, ..., numMinorBins and throws when
+  // their count disagrees (source/cudaNcorr.cu:174-180); with fewer than one
+  // pi bin its z cell would be 0 wide.
+  if (num_minor_bins < 1 || num_minor_bins > 4096)
+    return fail(NCORR_ERR_INVALID_ARGUMENT, "numMinorBins must be 1..4096");
+  for (int d = 0; d < 3; ++d)
+    if (!(box[d] > 0.0) || !std::isfinite(box[d]))
+      return fail(NCORR_ERR_INVALID_ARGUMENT, "box sides must be positive");
+  int dev_count = 0;
+  if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count <= 0)
+    return fail(NCORR_ERR_NO_DEVICE, "no CUDA device");
+  ncorr_handle* h = new ncorr_handle();
+  h->bin_type = NCORR_BIN_RPPI;
+  h->survey = is_survey ? 1 : 0;
+  for (int d = 0; d < 3; ++d) {
+    h->box[d] = box[d];
+    h->ori[d] = ori ? ori[d] : 0.0;
+  }
+  h->edges.assign(edges, edges + n_edges);
+  h->nb = n_edges - 1;
+  for (int i = 1; i < n_edges; ++i) h->mids.push_back((edges[i] + edges[i - 1]) / 2.0);
+  std::memset(&h->g, 0, sizeof(h->g));
+  std::memset(&h->stats, 0, sizeof(h->stats));
+  int rc = rppi_init(h, box, edges, n_edges, num_minor_bins, is_survey, ori);
+  if (rc) {
+    delete h;
+    return rc;
+  }
+  cudaGetDevice(&h->device);
+  cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+  for (int i = 0; i < 4 && e == cudaSuccess; ++i) e = cudaEventCreate(&h->ev[i]);
+  if (e != cudaSuccess) {
+    ncorr_destroy(h);
+    return fail(NCORR_ERR_CUDA, std::string("stream/event creation: ") + cudaGetErrorString(e));
+  }
+  *out = h;
+  return NCORR_OK;
 }
 
 void ncorr_destroy(ncorr_handle* h) {
@@ -412,7 +452,7 @@ void ncorr_destroy(ncorr_handle* h) {
   for (DevBuf* b : {&h->d_table, &h->d_flags, &h->d_wmax, &h->d_work, &h->d_bound, &h->d_hist,
                     &h->d_out, &h->d_stats, &h->d_total, &h->slab_e, &h->slab_m, &h->slab_p,
                     &h->slab_w, &h->xq, &h->xq_count, &h->d_args, &h->d_items, &h->d_cell_work,
-                    &h->d_feats, &h->q_item, &h->q_anchor})
+                    &h->d_feats, &h->q_item, &h->q_anchor, &h->rp_pos, &h->rp_ab, &h->rp_rel})
     b->release();
   h->order.release();
   for (auto& e : h->ev)
@@ -447,6 +487,9 @@ int ncorr_calculate_d1d2d3(ncorr_handle* h, const double* p1, int64_t n1, const 
       CU(cudaMemcpyAsync(b.p, src[r], ns[r] * sizeof(double4_16a), cudaMemcpyHostToDevice, st));
     dev[r] = b.as<double4_16a>();
   }
+  if (h->bin_type == NCORR_BIN_RPPI)
+    return rppi_run(h, dev[0], static_cast<int>(n1), dev[1], static_cast<int>(n2), dev[2], static_cast<int>(n3), st,
+                    p1, p2, p3);
   return run(h, dev[0], static_cast<int>(n1), dev[1], static_cast<int>(n2), dev[2],
              static_cast<int>(n3), st, p1, p2, p3);
 }
@@ -463,6 +506,10 @@ int ncorr_calculate_d1d2d3_device(ncorr_handle* h, const double* d_p1, int64_t n
     if (p && (reinterpret_cast<uintptr_t>(p) & 15u))
       return fail(NCORR_ERR_INVALID_ARGUMENT, "device catalogues must be 16-byte aligned");
   cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : h->stream;
+  if (h->bin_type == NCORR_BIN_RPPI)
+    return rppi_run(h, reinterpret_cast<const double4_16a*>(d_p1), static_cast<int>(n1),
+                    reinterpret_cast<const double4_16a*>(d_p2), static_cast<int>(n2),
+                    reinterpret_cast<const double4_16a*>(d_p3), static_cast<int>(n3), st, d_p1, d_p2, d_p3);
   return run(h, reinterpret_cast<const double4_16a*>(d_p1), static_cast<int>(n1),
              reinterpret_cast<const double4_16a*>(d_p2), static_cast<int>(n2),
              reinterpret_cast<const double4_16a*>(d_p3), static_cast<int>(n3), st, d_p1, d_p2, d_p3);
@@ -474,6 +521,8 @@ int64_t ncorr_num_out(const ncorr_handle* h) {
 
 int ncorr_num_bins(const ncorr_handle* h) { return h ? h->nb : 0; }
 
+int ncorr_num_pi_bins(const ncorr_handle* h) { return (h && h->bin_type == NCORR_BIN_RPPI) ? h->rg.npi : 0; }
+
 int ncorr_get_tri_bins_out(const ncorr_handle* h, double* out, int64_t cap) {
   if (!h || !out) return fail(NCORR_ERR_INVALID_ARGUMENT, "null argument");
   if (cap < static_cast<int64_t>(h->tri_bins_out.size()))
@@ -483,10 +532,12 @@ int ncorr_get_tri_bins_out(const ncorr_handle* h, double* out, int64_t cap) {
 }
 
 int ncorr_get_pi_bins_out(const ncorr_handle* h, double* out, int64_t cap, int64_t* n) {
-  (void)out;
-  (void)cap;
   if (!h) return fail(NCORR_ERR_INVALID_ARGUMENT, "null handle");
-  if (n) *n = 0;
+  const int64_t m = static_cast<int64_t>(h->pi_bins_out.size() / 2);
+  if (n) *n = m;
+  if (m == 0) return NCORR_OK;
+  if (!out || cap < 2 * m) return fail(NCORR_ERR_INVALID_ARGUMENT, "output capacity too small");
+  std::memcpy(out, h->pi_bins_out.data(), h->pi_bins_out.size() * sizeof(double));
   return NCORR_OK;
 }
 
@@ -510,6 +561,8 @@ int ncorr_set_schedule(ncorr_handle* h, int mode, const ncorr_sched* model) {
   if (!h) return fail(NCORR_ERR_INVALID_ARGUMENT, "null handle");
   if (mode != NCORR_SCHED_DYNAMIC && mode != NCORR_SCHED_STATIC && mode != NCORR_SCHED_LEARNED)
     return fail(NCORR_ERR_INVALID_ARGUMENT, "unknown schedule");
+  if (h->bin_type != NCORR_BIN_THREED && mode != NCORR_SCHED_DYNAMIC)
+    return fail(NCORR_ERR_NOT_IMPLEMENTED, "the rppi kernel takes anchors from a dynamic counter only");
   if (mode == NCORR_SCHED_LEARNED && !model)
     return fail(NCORR_ERR_INVALID_ARGUMENT, "the learned schedule needs a model");
   if (model && model->device != h->device)
@@ -531,6 +584,8 @@ int ncorr_set_tuning(ncorr_handle* h, int sub_j, int hist_copies) {
 
 int ncorr_set_record_work(ncorr_handle* h, int on) {
   if (!h) return fail(NCORR_ERR_INVALID_ARGUMENT, "null handle");
+  if (h->bin_type != NCORR_BIN_THREED && on)
+    return fail(NCORR_ERR_NOT_IMPLEMENTED, "work recording is implemented for the threeD bin type");
   h->record_work = on != 0;
   return NCORR_OK;
 }

@@ -12,6 +12,7 @@
 
 #include "../../include/ncorr_gb300.h"
 #include "engine.cuh"
+#include "rppi.cuh"
 #include "sched.cuh"
 #include "triangles.cuh"
 
@@ -46,6 +47,11 @@ inline int fail(int code, const std::string& msg) {
 // GB300, established by running the reference kernel on inputs built to
 // separate the candidates: fma(dz, dz, fma(dx, dx, dy*dy)).
 constexpr int kDefaultFmaPattern = 2;
+// Contractions of the rppi helpers under nvcc, established the same way:
+// sqrRpBox as fma(dx, dx, dy*dy) and dotProduct_d3 as
+// fma(a.z, b.z, fma(a.x, b.x, a.y*b.y)).
+constexpr int kDefaultRpPattern = 2;
+constexpr int kDefaultDotPattern = 2;
 
 // Budget of dynamic shared memory per CTA so that two CTAs share an SM, and
 // the largest CTA histogram kept in shared memory.
@@ -119,6 +125,7 @@ struct OrderBufs {
 }  // namespace ncorr_host
 
 struct ncorr_handle {
+  int bin_type = NCORR_BIN_THREED;
   int survey = 0;
   double box[3] = {0, 0, 0};
   double ori[3] = {0, 0, 0};
@@ -150,6 +157,12 @@ struct ncorr_handle {
   ncorr_host::OrderBufs order;
   std::vector<float> rec_feats;   // features of the last recorded call, ncell x 28
   std::vector<double> rec_work;   // its candidate pairs per cell of catalogue 1
+  // rppi bin type: geometry, piBinsOut_ table (2 per entry), per-CTA lists,
+  // weight of the last call's triangles indexed past triCountsAll_.
+  ncorr_gb300::RppiGeom rg;
+  std::vector<double> pi_bins_out;
+  ncorr_host::DevBuf rp_pos, rp_ab, rp_rel;
+  double rppi_overflow = 0.0;
 };
 
 // The scheduler's work-prediction MLP: parameters, Adam state and training
@@ -276,6 +289,12 @@ inline int grid_catalog(ncorr_handle* h, int ci, const double4_16a* d_in, int n,
   CU(cudaGetLastError());
   return NCORR_OK;
 }
+
+// The rppi bin type (rppi.cu).
+int rppi_init(ncorr_handle* h, const double box[3], const double* edges, int n_edges, int num_minor_bins,
+              int is_survey, const double ori[3]);
+int rppi_run(ncorr_handle* h, const double4_16a* d1, int n1, const double4_16a* d2, int n2, const double4_16a* d3,
+             int n3, cudaStream_t st, const void* key1, const void* key2, const void* key3);
 
 inline Catalog view(const CatDev& c) {
   Catalog v;

@@ -1,0 +1,58 @@
+// The (rp, pi) bin type: geometry and kernel arguments shared by rppi.cu and
+// the C ABI. The reference's second constructor (source/cudaNcorr.cu:159-216)
+// bins each side by its projected separation rp (nb bins, the given edges)
+// and, for the two shortest sides, by its line-of-sight separation pi (nPi
+// unit bins); its kernels are countTrianglesRppiBox (source/device.cu:317-379,
+// line of sight = z) and countTrianglesRppiSurvey (source/device.cu:434-505,
+// line of sight = the sum of the three position vectors).
+#pragma once
+#include "engine.cuh"
+
+namespace ncorr_gb300 {
+
+struct RppiGeom {
+  int nb;            // rp bins
+  int npi;           // unit pi bins (numPiBins_)
+  int survey;
+  int fma_pattern;   // contraction of sqrSep (survey)
+  int rp_pattern;    // contraction of sqrRpBox: 0 none, 1 fma(dy,dy,dx*dx), 2 fma(dx,dx,dy*dy)
+  int dot_pattern;   // contraction of dotProduct_d3 (sqrSep numbering)
+  int nc[3];
+  double box[3];
+  double cell[3];    // box: (rpMax, rpMax, piMax); survey: rMax = sqrtf(rpMax^2 + piMax^2) per axis
+  double ori_x;      // d_ori as the survey kernel sees it: (ori.x, 0, 0)
+  double sqr_rpmax, sqr_rpmin, sqr_pimax;
+  double sqr_rmax, sqr_rmin;  // survey pair cut: rpMax^2 + piMax^2 and 0
+  double sqr_bins[kMaxEdges];
+  // FP32 prefilter on anchor-relative offsets: a candidate whose estimate
+  // passes one of these thresholds is certainly cut by the reference.
+  float f_pi_hi;     // box: dz^2 estimate > f_pi_hi  => pi^2 >= piMax^2
+  float f_rp_hi;     // box: rp^2 estimate > f_rp_hi  => rp^2 >= rpMax^2
+  float f_rp_lo;     // box: rp^2 estimate < f_rp_lo  => rp^2 <= rpMin^2
+  float f_s_hi;      // survey: s^2 estimate > f_s_hi => s^2 >= sqrRMax
+  long long nbins;   // nb^3 * nPi^2
+};
+
+struct RppiArgs {
+  RppiGeom g;
+  const double4_16a* a_pd;  // anchors (cell order)
+  int n1;
+  const double4_16a* pd2;
+  const int* start2;
+  const int* count2;
+  const double4_16a* pd3;
+  const int* start3;
+  const int* count3;
+  // Per-CTA neighbour lists (two lists of `cap` entries per CTA).
+  double4_16a* l_pos;  // neighbour (its image in a box), weight
+  double2* l_ab;       // box: (rp^2, pi^2) to the anchor; survey: (sqrS, 0)
+  float4* l_rel;       // FP32 anchor-relative offset
+  int cap;
+  unsigned long long* hist_u;  // nbins + 1 counts; [nbins] collects indices past the end
+  double* hist_w;              // nbins + 1 weighted sums (same layout)
+  int* work;
+  int* flags;
+  unsigned long long* stats;   // [0] anchors, [1] scanned, [2] candidate pairs, [3] exact evaluations
+};
+
+}  // namespace ncorr_gb300

@@ -10,8 +10,7 @@
 // Differences from the reference, all on inputs where the reference has
 // undefined behaviour: points outside the reference's cell grid, non-finite
 // values, and edges that are not strictly increasing and non-negative are
-// rejected with std::runtime_error. The rppi constructor throws (bin type not
-// implemented by this engine). Instances hold a device handle and are
+// rejected with std::runtime_error. Instances hold a device handle and are
 // movable, not copyable.
 #ifndef _CUDANCORR_HPP_
 #define _CUDANCORR_HPP_
@@ -36,7 +35,7 @@ class ncorr {
     check(ncorr_create(b, bin_type, bins.data(), static_cast<int>(bins.size()), isSurvey ? 1 : 0, o, &h_));
   }
 
-  // include/cudaNcorr.hpp:15 of the reference (rppi): not implemented here.
+  // include/cudaNcorr.hpp:15 of the reference (rppi).
   ncorr(double3 box, int bin_type, std::vector<double>& bins, int numMinorBins, bool isSurvey,
         double3 ori) {
     const double b[3] = {box.x, box.y, box.z};
@@ -72,16 +71,25 @@ class ncorr {
     std::vector<double> flat(static_cast<size_t>(3 * n));
     check(ncorr_get_tri_bins_out(h_, flat.data(), 3 * n));
     std::vector<double3> out(static_cast<size_t>(n));
-    for (int64_t i = 0; i < n; ++i) out[i] = make_double3(flat[3 * i], flat[3 * i + 1], flat[3 * i + 2]);
+    for (int64_t i = 0; i < n; ++i) out[i] = double3{flat[3 * i], flat[3 * i + 1], flat[3 * i + 2]};
     return out;
   }
 
-  // include/cudaNcorr.hpp:23 of the reference: empty for the threeD bin type.
+  // include/cudaNcorr.hpp:23 of the reference: (l, m) pi bins of every
+  // output entry for rppi, empty for threeD.
   std::vector<double2> getPiBinsOut() const {
     int64_t n = 0;
-    double dummy = 0.0;
-    check(ncorr_get_pi_bins_out(h_, &dummy, 0, &n));
-    return std::vector<double2>(static_cast<size_t>(n));
+    if (ncorr_num_pi_bins(h_) == 0) {
+      double dummy = 0.0;
+      check(ncorr_get_pi_bins_out(h_, &dummy, 0, &n));
+      return std::vector<double2>(static_cast<size_t>(n));
+    }
+    const int64_t m = ncorr_num_out(h_);
+    std::vector<double> flat(static_cast<size_t>(2 * m));
+    check(ncorr_get_pi_bins_out(h_, flat.data(), 2 * m, &n));
+    std::vector<double2> out(static_cast<size_t>(n));
+    for (int64_t i = 0; i < n; ++i) out[i] = double2{flat[2 * i], flat[2 * i + 1]};
+    return out;
   }
 
   // include/cudaNcorr.hpp:25 of the reference.
@@ -91,10 +99,12 @@ class ncorr {
     return out;
   }
 
-  // The full nb^3 histogram (the reference's private triCountsAll_).
+  // The full histogram (the reference's private triCountsAll_): nb^3
+  // entries, nb^3 * numPiBins^2 for rppi.
   std::vector<double> getTriCountsAll() const {
     const int nb = ncorr_num_bins(h_);
-    std::vector<double> out(static_cast<size_t>(nb) * nb * nb);
+    const int npi = ncorr_num_pi_bins(h_);
+    std::vector<double> out(static_cast<size_t>(nb) * nb * nb * (npi > 0 ? static_cast<size_t>(npi) * npi : 1));
     check(ncorr_get_tri_counts_all(h_, out.data(), static_cast<int64_t>(out.size())));
     return out;
   }

@@ -1,7 +1,8 @@
 /*
  * C ABI of the GB300 three-point correlation engine.
  *
- * This is the drop-in boundary for cudaNcorr's threeD counting path. Each
+ * This is the drop-in boundary for cudaNcorr's counting path (threeD and rppi
+ * bin types). Each
  * entry point replaces one member of the reference's C++ class `ncorr`
  * (include/cudaNcorr.hpp of cudaNcorr) or of its survey helpers
  * (include/survey.hpp, source/survey.cu); the cited lines are that project's.
@@ -32,7 +33,7 @@ extern "C" {
 typedef enum ncorr_status {
   NCORR_OK = 0,
   NCORR_ERR_INVALID_ARGUMENT = 1, /* bad box, edges, sizes or null pointers */
-  NCORR_ERR_NOT_IMPLEMENTED = 2,  /* rppi / smu bin types */
+  NCORR_ERR_NOT_IMPLEMENTED = 2,  /* a feature this engine lacks for the handle's bin type */
   NCORR_ERR_CUDA = 3,             /* a CUDA call failed; see ncorr_last_error() */
   NCORR_ERR_OUT_OF_GRID = 4,      /* a point outside the reference's cell grid, or non-finite */
   NCORR_ERR_CAPACITY = 5,         /* internal list capacity exceeded */
@@ -64,6 +65,9 @@ typedef struct ncorr_stats {
                               where all three vertices see each other identically) */
   int grid_ctas;           /* persistent CTAs of the triangle kernel */
   int list_capacity;       /* shared-memory neighbour-list capacity */
+  double overflow;         /* rppi: count (or weight) of triangles whose reference index lies
+                              past triCountsAll_ (pi bin numMinorBins from FP32 rounding);
+                              the reference writes those out of bounds */
 } ncorr_stats;
 
 /* ncorr::ncorr(double3 box, int bin_type, std::vector<double>& bins,
@@ -78,8 +82,15 @@ int ncorr_create(const double box[3], int bin_type, const double* edges, int n_e
 
 /* ncorr::ncorr(double3 box, int bin_type, std::vector<double>& bins,
  *              int numMinorBins, bool isSurvey, double3 ori)
- * include/cudaNcorr.hpp:15, source/cudaNcorr.cu:159-216. The rppi bin type is
- * not implemented by this engine: returns NCORR_ERR_NOT_IMPLEMENTED. */
+ * include/cudaNcorr.hpp:15, source/cudaNcorr.cu:159-216: the rppi bin type.
+ * Sides are binned by rp (edges, as for threeD) and the two shortest by pi in
+ * num_minor_bins unit bins [0,1), [1,2), ...; piMax = num_minor_bins. Box
+ * cells are (rpMax, rpMax, piMax), line of sight z; survey cells are cubes of
+ * sqrtf(rpMax^2 + piMax^2) (FP32, as the reference), line of sight the sum
+ * of the three positions minus (ori.x, 0, 0) (the reference uploads only
+ * ori.x). triCountsAll_ has nb^3 * num_minor_bins^2 entries indexed
+ * idxPi2 + idxPi1*nPi + idx3*nPi^2 + idx2*nb*nPi^2 + idx1*nb^2*nPi^2.
+ * bin_type other than NCORR_BIN_RPPI is rejected as the reference throws. */
 int ncorr_create_rppi(const double box[3], int bin_type, const double* edges, int n_edges,
                       int num_minor_bins, int is_survey, const double ori[3], ncorr_handle** out);
 
@@ -108,20 +119,25 @@ int64_t ncorr_num_out(const ncorr_handle* h);
 /* Number of bins per side. */
 int ncorr_num_bins(const ncorr_handle* h);
 
+/* numPiBins_ of an rppi handle (source/cudaNcorr.cu:178); 0 for threeD. */
+int ncorr_num_pi_bins(const ncorr_handle* h);
+
 /* ncorr::getTriBinsOut() (include/cudaNcorr.hpp:21, source/cudaNcorr.cu:106-108):
  * num_out x 3 bin mids into out (capacity cap doubles). */
 int ncorr_get_tri_bins_out(const ncorr_handle* h, double* out, int64_t cap);
 
 /* ncorr::getPiBinsOut() (include/cudaNcorr.hpp:23, source/cudaNcorr.cu:110-112):
- * always empty for the threeD bin type; *n receives 0. */
+ * rppi: num_out x 2 pi bins (l, m) into out (capacity cap doubles), *n = num_out;
+ * threeD: empty, *n = 0. */
 int ncorr_get_pi_bins_out(const ncorr_handle* h, double* out, int64_t cap, int64_t* n);
 
 /* ncorr::getTriCountsOut() (include/cudaNcorr.hpp:25, source/cudaNcorr.cu:114-116):
  * num_out counts of the last calculation. */
 int ncorr_get_tri_counts_out(const ncorr_handle* h, double* out, int64_t cap);
 
-/* The full nb^3 histogram triCountsAll_ (private in the reference,
- * include/cudaNcorr.hpp:49), of which getTriCountsOut is a compaction. */
+/* The full histogram triCountsAll_ (private in the reference,
+ * include/cudaNcorr.hpp:49), of which getTriCountsOut is a compaction:
+ * nb^3 entries (threeD) or nb^3 * numPiBins^2 (rppi). */
 int ncorr_get_tri_counts_all(const ncorr_handle* h, double* out, int64_t cap);
 
 /* Counters and timings of the last calculation. */
@@ -151,6 +167,31 @@ int survey_convert_coordinates(const double cosmo[3], const double* in, int64_t 
 /* logspace(start, end, n) (include/utils.hpp:9, source/utils.cu:16-27):
  * n log-spaced bin edges from start to end. */
 int ncorr_logspace(double start, double end, int n, double* out);
+
+/* writeToFileThreeD(filename, triBins, counts) (include/utils.hpp:15-19,
+ * source/utils.cu:161-181): one row "r1 r2 r3 count" per entry, each value
+ * with 6 decimals. tri_bins: n x 3 (getTriBinsOut), counts: n. */
+int ncorr_write_three_d(const char* filename, const double* tri_bins, const double* counts, int64_t n);
+
+/* writeToFileRppi(filename, triBins, piBins, counts) (include/utils.hpp:21-26,
+ * source/utils.cu:183-208): rows "r1 r2 r3 pi1 pi2 count". pi_bins: n x 2. */
+int ncorr_write_rppi(const char* filename, const double* tri_bins, const double* pi_bins, const double* counts,
+                     int64_t n);
+
+/* readCatalogTxt(filename, box, pos_columns) (include/utils.hpp:36-40,
+ * source/utils.cu:119-159): whitespace-separated text, one point per line;
+ * pos_columns[0..3] name the columns of x, y, z and w. A coordinate outside
+ * [0, box] fails with NCORR_ERR_OUT_OF_GRID and the line number, as the
+ * reference throws; a line without one of the four columns fails too (the
+ * reference leaves that point uninitialised). *n receives the number of
+ * points; out (capacity cap points of 4 doubles) may be null to size it. */
+int ncorr_read_catalog_txt(const char* filename, const double box[3], const int pos_columns[4], double* out,
+                           int64_t cap, int64_t* n);
+
+/* generateRandomCatalog(Np, box) (include/utils.hpp:11, source/utils.cu:41-52):
+ * n points uniform in [0, box) per axis, weight 1. The reference seeds from
+ * the clock and the thread number; here the stream depends only on `seed`. */
+int ncorr_random_catalog(int64_t n, const double box[3], uint64_t seed, double* out);
 
 /* Triangle count without any device allocation; no counterpart in the
  * reference. For callers that must not allocate device memory -- code given a

@@ -43,8 +43,8 @@ class survey {
   void prep_cat_survey(std::vector<double4>& catalog, double3& box, double3& ori) {
     double b[3], o[3];
     check(survey_prep_cat(reinterpret_cast<double*>(catalog.data()), static_cast<int64_t>(catalog.size()), b, o));
-    box = make_double3(b[0], b[1], b[2]);
-    ori = make_double3(o[0], o[1], o[2]);
+    box = double3{b[0], b[1], b[2]};
+    ori = double3{o[0], o[1], o[2]};
   }
 
   void prep_cat_survey(std::vector<double4>& catalog1, std::vector<double4>& catalog2, double3& box,
@@ -52,8 +52,8 @@ class survey {
     double b[3], o[3];
     check(survey_prep_cat2(reinterpret_cast<double*>(catalog1.data()), static_cast<int64_t>(catalog1.size()),
                            reinterpret_cast<double*>(catalog2.data()), static_cast<int64_t>(catalog2.size()), b, o));
-    box = make_double3(b[0], b[1], b[2]);
-    ori = make_double3(o[0], o[1], o[2]);
+    box = double3{b[0], b[1], b[2]};
+    ori = double3{o[0], o[1], o[2]};
   }
 
  private:

@@ -6,9 +6,10 @@
 // the product links or calls it.
 //
 // Parity status: pinned. The reference ships no tests or golden files, so the
-// restatement is pinned against outputs of the reference's own kernel
+// restatement is pinned against outputs of the reference's own kernels
 // (source/device.cu, compiled unmodified and run through oracle/ref_runner.cu)
-// on seeded inputs, recorded under tests/golden/.
+// on seeded inputs, recorded under tests/golden/ (threeD and rppi, box and
+// survey).
 //
 // Build: -O2 -fopenmp -ffp-contract=off (no implicit FMA: every fused
 // multiply-add below is spelled out with std::fma, to restate exactly the
@@ -28,6 +29,15 @@
 //   source/device.cu:381-431     countTrianglesThreeDSurvey
 //   source/survey.cu:60-128      find_min_max_elements / shift_catalog / prep_cat_survey
 //   source/utils.cu:16-27        logspace
+// and of its rppi bin type:
+//   source/cudaNcorr.cu:88-105   prepTriCountsOutRppi
+//   source/cudaNcorr.cu:159-216  rppi constructor (pi bins, cells, rMax = sqrtf)
+//   source/device.cu:23-25       dotProduct_d3 (six contraction candidates)
+//   source/device.cu:38-68       sqrRpBox / sqrPiBox / getLOS / getSqrSdotL /
+//                                getSqrRpSqrPi
+//   source/device.cu:203-255     getTriangleIndexRppi
+//   source/device.cu:317-379     countTrianglesRppiBox
+//   source/device.cu:434-505     countTrianglesRppiSurvey
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -418,6 +428,430 @@ int run(const Geometry& g, const Pt* p1, long n1, const Pt* p2, long n2, const P
   return 0;
 }
 
+
+// ======================================================================= rppi
+// The (rp, pi) bin type: ncorr's second constructor (source/cudaNcorr.cu:159-216)
+// with the kernels countTrianglesRppiBox (source/device.cu:317-379) and
+// countTrianglesRppiSurvey (source/device.cu:434-505).
+
+// sqrRpBox (source/device.cu:38-43): dx*dx + dy*dy under one of the three
+// ways a compiler may contract it.
+enum RpPattern {
+  kRpNoFma = 0,   // dx*dx + dy*dy, every operation rounded
+  kRpFmaDy = 1,   // fma(dy, dy, dx*dx)
+  kRpFmaDx = 2,   // fma(dx, dx, dy*dy)
+};
+
+inline double rp_sum(int pat, double dx, double dy) {
+  if (pat == kRpNoFma) {
+    double a = dx * dx;
+    double b = dy * dy;
+    return a + b;
+  }
+  if (pat == kRpFmaDy) return std::fma(dy, dy, dx * dx);
+  return std::fma(dx, dx, dy * dy);
+}
+
+// dotProduct_d3 (source/device.cu:23-25): a.x*b.x + a.y*b.y + a.z*b.z with
+// the same six contraction candidates as sqrSep (SqrSepPattern numbering).
+inline double dot3(int pat, const double a[3], const double b[3]) {
+  switch (pat) {
+    case kNoFma: {
+      double x = a[0] * b[0];
+      double y = a[1] * b[1];
+      double z = a[2] * b[2];
+      return (x + y) + z;
+    }
+    case kFmaInnerDy: return std::fma(a[2], b[2], std::fma(a[1], b[1], a[0] * b[0]));
+    case kFmaInnerDx: return std::fma(a[2], b[2], std::fma(a[0], b[0], a[1] * b[1]));
+    case kFmaOuterOnly: {
+      double x = a[0] * b[0];
+      double y = a[1] * b[1];
+      return std::fma(a[2], b[2], x + y);
+    }
+    case kFmaInnerDyOnly: {
+      double z = a[2] * b[2];
+      return std::fma(a[1], b[1], a[0] * b[0]) + z;
+    }
+    default: {
+      double z = a[2] * b[2];
+      return std::fma(a[0], b[0], a[1] * b[1]) + z;
+    }
+  }
+}
+
+struct RppiGeometry {
+  Geometry g;            // bins, shifts, nc, box, survey flag (cell unused)
+  int npi = 0;           // numPiBins_
+  double cellv[3] = {0, 0, 0};
+  double sqr_rpmax = 0, sqr_rpmin = 0, sqr_pimax = 0;
+  double sqr_rmax = 0;   // rpMax^2 + piMax^2 (source/cudaNcorr.cu:182)
+  double sqr_rmin = 0;   // never set by the reference (see make_rppi_geometry)
+  double ori[3] = {0, 0, 0};  // d_ori as the kernels see it: (ori.x, 0, 0)
+  int rp_pat = kRpFmaDx;
+  int dot_pat = kFmaInnerDx;
+};
+
+// The rppi constructor (source/cudaNcorr.cu:159-216). Pi bins are unit wide,
+// 0..numMinorBins; the box grid uses cells (rpMax, rpMax, piMax), the survey
+// grid cubes of rMax = sqrtf(rpMax^2 + piMax^2) evaluated in FP32
+// (source/cudaNcorr.cu:183, float sqrtf of the double). sqrRMin_ is left
+// uninitialised there yet uploaded to d_sqrRMin and used by the survey kernel
+// (source/cudaNcorr.cu:229, source/device.cu:459, :466); any value in
+// [0, rpMin^2] gives the same counts, because every side that counts has
+// sqrS >= sqrRp > rpMin^2, so it is defined as 0 here. The reference uploads
+// only d_ori.x (sizeof(double) at source/cudaNcorr.cu:254), so the kernels see
+// (ori.x, 0, 0).
+int make_rppi_geometry(const double* box, const double* edges, int n_edges, int npi, int is_survey,
+                       const double* ori, RppiGeometry* r) {
+  Geometry& g = r->g;
+  if (n_edges < 2 || npi < 1 || npi > 4096) return -1;
+  for (int i = 0; i < n_edges; ++i)
+    if (!std::isfinite(edges[i])) return -1;
+  if (edges[0] < 0.0) return -1;
+  for (int i = 1; i < n_edges; ++i)
+    if (!(edges[i] > edges[i - 1])) return -1;
+  for (int d = 0; d < 3; ++d)
+    if (!(box[d] > 0.0) || !std::isfinite(box[d])) return -1;
+  g.nb = n_edges - 1;
+  g.sqr_bins.resize(n_edges);
+  for (int i = 0; i < n_edges; ++i) g.sqr_bins[i] = edges[i] * edges[i];
+  const double rpmax = edges[n_edges - 1], rpmin = edges[0];
+  r->npi = npi;
+  const double pimax = static_cast<double>(npi);
+  r->sqr_rpmax = rpmax * rpmax;
+  r->sqr_rpmin = rpmin * rpmin;
+  r->sqr_pimax = pimax * pimax;
+  r->sqr_rmax = rpmax * rpmax + pimax * pimax;
+  r->sqr_rmin = 0.0;
+  const double rmax = static_cast<double>(std::sqrt(static_cast<float>(r->sqr_rmax)));
+  g.survey = is_survey != 0;
+  if (g.survey) {
+    r->cellv[0] = r->cellv[1] = r->cellv[2] = rmax;
+  } else {
+    r->cellv[0] = r->cellv[1] = rpmax;
+    r->cellv[2] = pimax;
+  }
+  for (int d = 0; d < 3; ++d) {
+    g.box[d] = box[d];
+    g.cell[d] = r->cellv[d];
+    double n = std::ceil(box[d] / r->cellv[d]);
+    if (n > 4096.0) return -2;
+    g.nc[d] = static_cast<int>(n);
+  }
+  r->ori[0] = (g.survey && ori) ? ori[0] : 0.0;
+  r->ori[1] = 0.0;
+  r->ori[2] = 0.0;
+  int s = 0;
+  for (int i = -1; i <= 1; ++i)
+    for (int j = -1; j <= 1; ++j)
+      for (int k = -1; k <= 1; ++k) {
+        g.shifts[s][0] = i;
+        g.shifts[s][1] = j;
+        g.shifts[s][2] = k;
+        ++s;
+      }
+  return 0;
+}
+
+// getTriangleIndexRppi (source/device.cu:203-255): sort the three sides by
+// rp^2 carrying their pi^2 along, FP32 sqrtf triangle test, rp bin of each
+// side, unit pi bins floor(sqrtf(pi^2)) of the two shortest sides, flat index
+// idxPi2 + idxPi1*nPi + idx3*nPi^2 + idx2*nb*nPi^2 + idx1*nb^2*nPi^2. The
+// returned index is the reference's even where it lands outside the nb^3*nPi^2
+// histogram (a pi^2 just below piMax^2 whose FP32 square root rounds up to
+// piMax gives pi bin nPi).
+inline long rppi_index(double r1, double r2, double r3, double q1, double q2, double q3,
+                       const std::vector<double>& sb, int nb, int npi) {
+  double t;
+  if (r1 > r2) {
+    t = r1; r1 = r2; r2 = t;
+    t = q1; q1 = q2; q2 = t;
+  }
+  if (r1 > r3) {
+    t = r1; r1 = r3; r3 = t;
+    t = q1; q1 = q3; q3 = t;
+  }
+  if (r2 > r3) {
+    t = r2; r2 = r3; r3 = t;
+    t = q2; q2 = q3; q3 = t;
+  }
+  float s1 = std::sqrt(static_cast<float>(r1));
+  float s2 = std::sqrt(static_cast<float>(r2));
+  float s3 = std::sqrt(static_cast<float>(r3));
+  float sum = s1 + s2;
+  if (sum <= s3) return -1;
+  int idx[3] = {-1, -1, -1};
+  const double r[3] = {r1, r2, r3};
+  for (int i = 0; i < nb; ++i)
+    for (int m = 0; m < 3; ++m)
+      if (r[m] >= sb[i] && r[m] < sb[i + 1]) idx[m] = i;
+  if (idx[0] < 0 || idx[1] < 0 || idx[2] < 0) return -1;  // unreachable for in-range sides
+  const long p1 = static_cast<long>(std::floor(std::sqrt(static_cast<float>(q1))));
+  const long p2 = static_cast<long>(std::floor(std::sqrt(static_cast<float>(q2))));
+  const long P = npi, B = nb;
+  return p2 + p1 * P + idx[2] * P * P + idx[1] * B * P * P + idx[0] * B * B * P * P;
+}
+
+// Histogram of an rppi count plus the weight that the reference writes past
+// its end (index >= nb^3 * nPi^2).
+struct RppiHist {
+  std::vector<Acc> bins;
+  Acc overflow;
+};
+
+inline void rppi_add(RppiHist& h, long idx, double w) {
+  if (idx < 0) return;
+  if (idx < static_cast<long>(h.bins.size()))
+    h.bins[idx].add(w);
+  else
+    h.overflow.add(w);
+}
+
+inline void shifted(const Pt& p, const double sh[3], Pt* q) {
+  *q = p;
+  q->x += sh[0];
+  q->y += sh[1];
+  q->z += sh[2];
+}
+
+// countTrianglesRppiSurvey's per-triangle body (source/device.cu:460-500)
+// after its sqrS range tests: line of sight from getLOS (:45-56), squared
+// projections from getSqrSdotL (:58-63), pi^2 = (s.L)^2 / L^2 and
+// rp^2 = s^2 - pi^2 (getSqrRpSqrPi, :65-68), the three projection cuts, then
+// the rp and pi range tests. Returns the flat index or -1.
+inline long survey_rppi_body(const RppiGeometry& R, const Pt& p1, const Pt& p2, const Pt& p3, double s1,
+                             double s2, double s3) {
+  const double* o = R.ori;
+  const double a[3] = {p1.x - o[0], p1.y - o[1], p1.z - o[2]};
+  const double b[3] = {p2.x - o[0], p2.y - o[1], p2.z - o[2]};
+  const double c[3] = {p3.x - o[0], p3.y - o[1], p3.z - o[2]};
+  const double los[3] = {a[0] + b[0] + c[0], a[1] + b[1] + c[1], a[2] + b[2] + c[2]};
+  const double sqrL = dot3(R.dot_pat, los, los);
+  const double pm = R.sqr_pimax * sqrL;
+  const double d12[3] = {p1.x - p2.x, p1.y - p2.y, p1.z - p2.z};
+  double t = dot3(R.dot_pat, los, d12);
+  const double q1 = t * t;
+  if (pm < q1) return -1;
+  const double d13[3] = {p1.x - p3.x, p1.y - p3.y, p1.z - p3.z};
+  t = dot3(R.dot_pat, los, d13);
+  const double q2 = t * t;
+  if (pm < q2) return -1;
+  const double d23[3] = {p2.x - p3.x, p2.y - p3.y, p2.z - p3.z};
+  t = dot3(R.dot_pat, los, d23);
+  const double q3 = t * t;
+  if (pm < q3) return -1;
+  const double pi1 = q1 / sqrL, pi2 = q2 / sqrL, pi3 = q3 / sqrL;
+  const double rp1 = s1 - pi1, rp2 = s2 - pi2, rp3 = s3 - pi3;
+  if (rp1 < R.sqr_rpmax && rp2 < R.sqr_rpmax && rp3 < R.sqr_rpmax && rp1 > R.sqr_rpmin &&
+      rp2 > R.sqr_rpmin && rp3 > R.sqr_rpmin && pi1 < R.sqr_pimax && pi2 < R.sqr_pimax)
+    return rppi_index(rp1, rp2, rp3, pi1, pi2, pi3, R.g.sqr_bins, R.g.nb, R.npi);
+  return -1;
+}
+
+// Literal restatement of both rppi loop nests (source/device.cu:317-379 and
+// :434-505): for every anchor, 27 cells for p2 and, for each p2 that passes,
+// 27 cells again for p3.
+template <int P>
+void count_rppi_literal(const RppiGeometry& R, const Pt* p1, long n1, const Grid& g2, const Grid& g3,
+                        int nthreads, RppiHist* out) {
+  const Geometry& g = R.g;
+  const long nbin = static_cast<long>(g.nb) * g.nb * g.nb * R.npi * R.npi;
+  std::vector<RppiHist> part(nthreads);
+  for (auto& h : part) h.bins.assign(nbin, Acc());
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 16)
+  for (long a = 0; a < n1; ++a) {
+    RppiHist& h = part[omp_get_thread_num()];
+    const Pt q1 = p1[a];
+    int home[3];
+    anchor_cell(g, q1, home);
+    for (int s2 = 0; s2 < 27; ++s2) {
+      double sh2[3];
+      long c2 = neighbour_cell(g, home, s2, sh2);
+      if (c2 < 0) continue;
+      for (long j = g2.start[c2]; j < g2.start[c2] + g2.count[c2]; ++j) {
+        Pt q2;
+        if (g.survey) {
+          q2 = g2.pts[j];
+        } else {
+          shifted(g2.pts[j], sh2, &q2);
+        }
+        double pi1 = 0, rp1 = 0, s1 = 0;
+        if (g.survey) {
+          s1 = sqr_sep<P>(q1, q2);
+          if (!(s1 < R.sqr_rmax && s1 > R.sqr_rmin)) continue;
+        } else {
+          const double dz = q1.z - q2.z;
+          pi1 = dz * dz;
+          if (!(pi1 < R.sqr_pimax)) continue;
+          rp1 = rp_sum(R.rp_pat, q1.x - q2.x, q1.y - q2.y);
+          if (!(rp1 < R.sqr_rpmax && rp1 > R.sqr_rpmin)) continue;
+        }
+        for (int s3 = 0; s3 < 27; ++s3) {
+          double sh3[3];
+          long c3 = neighbour_cell(g, home, s3, sh3);
+          if (c3 < 0) continue;
+          for (long l = g3.start[c3]; l < g3.start[c3] + g3.count[c3]; ++l) {
+            Pt q3;
+            if (g.survey) {
+              q3 = g3.pts[l];
+              const double s2v = sqr_sep<P>(q1, q3);
+              const double s3v = sqr_sep<P>(q2, q3);
+              if (s2v < R.sqr_rmax && s3v < R.sqr_rmax && s2v > R.sqr_rmin && s3v > R.sqr_rmin) {
+                long t = survey_rppi_body(R, q1, q2, q3, s1, s2v, s3v);
+                if (t != -1) rppi_add(h, t, q1.w * q2.w * q3.w);
+              }
+            } else {
+              shifted(g3.pts[l], sh3, &q3);
+              double dz2 = q1.z - q3.z, dz3 = q2.z - q3.z;
+              const double pi2 = dz2 * dz2, pi3 = dz3 * dz3;
+              if (pi2 < R.sqr_pimax && pi3 < R.sqr_pimax) {
+                const double rp2 = rp_sum(R.rp_pat, q1.x - q3.x, q1.y - q3.y);
+                const double rp3 = rp_sum(R.rp_pat, q2.x - q3.x, q2.y - q3.y);
+                if (rp2 < R.sqr_rpmax && rp3 < R.sqr_rpmax && rp2 > R.sqr_rpmin && rp3 > R.sqr_rpmin) {
+                  long t = rppi_index(rp1, rp2, rp3, pi1, pi2, pi3, g.sqr_bins, g.nb, R.npi);
+                  if (t != -1) rppi_add(h, t, q1.w * q2.w * q3.w);
+                }
+              }
+            }
+          }
+        }
+      }
+    }
+  }
+  out->bins.assign(nbin, Acc());
+  out->overflow = Acc();
+  for (int t = 0; t < nthreads; ++t) {
+    for (long b = 0; b < nbin; ++b) {
+      out->bins[b].add(part[t].bins[b].s);
+      out->bins[b].add(part[t].bins[b].c);
+    }
+    out->overflow.add(part[t].overflow.s);
+    out->overflow.add(part[t].overflow.c);
+  }
+}
+
+struct RNbr {
+  Pt p;            // neighbour (its periodic image in a box)
+  double a, b;     // box: rp^2, pi^2 to the anchor; survey: sqrS, unused
+};
+
+// The anchor's neighbours that pass the reference's p2 cut. The p3 cuts
+// against the anchor are the same tests (pi^2 < piMax^2 and rp^2 in range in
+// a box, sqrS in range in a survey), so one list serves both roles.
+template <int P>
+inline void gather_rppi(const RppiGeometry& R, const Pt& q1, const int home[3], const Grid& gr,
+                        std::vector<RNbr>* lst) {
+  const Geometry& g = R.g;
+  lst->clear();
+  for (int s = 0; s < 27; ++s) {
+    double sh[3];
+    long c = neighbour_cell(g, home, s, sh);
+    if (c < 0) continue;
+    for (long j = gr.start[c]; j < gr.start[c] + gr.count[c]; ++j) {
+      if (g.survey) {
+        const Pt& q = gr.pts[j];
+        const double s1 = sqr_sep<P>(q1, q);
+        if (s1 < R.sqr_rmax && s1 > R.sqr_rmin) lst->push_back({q, s1, 0.0});
+      } else {
+        Pt q;
+        shifted(gr.pts[j], sh, &q);
+        const double dz = q1.z - q.z;
+        const double pi = dz * dz;
+        if (!(pi < R.sqr_pimax)) continue;
+        const double rp = rp_sum(R.rp_pat, q1.x - q.x, q1.y - q.y);
+        if (rp < R.sqr_rpmax && rp > R.sqr_rpmin) lst->push_back({q, rp, pi});
+      }
+    }
+  }
+}
+
+// Same arithmetic as count_rppi_literal with each anchor's lists gathered
+// once (the reference's inner walk recomputes the anchor-p3 terms for every
+// p2 and gets the same values).
+template <int P>
+void count_rppi_lists(const RppiGeometry& R, const Pt* p1, long n1, const Grid& g2, const Grid& g3,
+                      bool same23, int nthreads, RppiHist* out) {
+  const Geometry& g = R.g;
+  const long nbin = static_cast<long>(g.nb) * g.nb * g.nb * R.npi * R.npi;
+  std::vector<RppiHist> part(nthreads);
+  for (auto& h : part) h.bins.assign(nbin, Acc());
+#pragma omp parallel num_threads(nthreads)
+  {
+    std::vector<RNbr> l2, l3;
+    RppiHist& h = part[omp_get_thread_num()];
+#pragma omp for schedule(dynamic, 4)
+    for (long a = 0; a < n1; ++a) {
+      const Pt q1 = p1[a];
+      int home[3];
+      anchor_cell(g, q1, home);
+      gather_rppi<P>(R, q1, home, g2, &l2);
+      const std::vector<RNbr>* pl3 = &l2;
+      if (!same23) {
+        gather_rppi<P>(R, q1, home, g3, &l3);
+        pl3 = &l3;
+      }
+      const std::vector<RNbr>& L3 = *pl3;
+      for (const RNbr& b : l2) {
+        for (const RNbr& c : L3) {
+          long t = -1;
+          if (g.survey) {
+            const double s3 = sqr_sep<P>(b.p, c.p);
+            if (s3 < R.sqr_rmax && s3 > R.sqr_rmin) t = survey_rppi_body(R, q1, b.p, c.p, b.a, c.a, s3);
+          } else {
+            const double dz = b.p.z - c.p.z;
+            const double pi3 = dz * dz;
+            if (pi3 < R.sqr_pimax) {
+              const double rp3 = rp_sum(R.rp_pat, b.p.x - c.p.x, b.p.y - c.p.y);
+              if (rp3 < R.sqr_rpmax && rp3 > R.sqr_rpmin)
+                t = rppi_index(b.a, c.a, rp3, b.b, c.b, pi3, g.sqr_bins, g.nb, R.npi);
+            }
+          }
+          if (t != -1) rppi_add(h, t, q1.w * b.p.w * c.p.w);
+        }
+      }
+    }
+  }
+  out->bins.assign(nbin, Acc());
+  out->overflow = Acc();
+  for (int t = 0; t < nthreads; ++t) {
+    for (long b = 0; b < nbin; ++b) {
+      out->bins[b].add(part[t].bins[b].s);
+      out->bins[b].add(part[t].bins[b].c);
+    }
+    out->overflow.add(part[t].overflow.s);
+    out->overflow.add(part[t].overflow.c);
+  }
+}
+
+template <int P>
+int run_rppi(const RppiGeometry& R, const Pt* p1, long n1, const Pt* p2, long n2, const Pt* p3, long n3,
+             int nthreads, int variant, double* hist, double* overflow) {
+  const Geometry& g = R.g;
+  int ijk[3];
+  for (long i = 0; i < n1; ++i) {
+    if (host_cell(g, p1[i], ijk) < 0) return -3;
+    if (!anchor_cell(g, p1[i], ijk)) return -3;
+  }
+  Grid g2, g3;
+  int rc = build_grid(g, p2, n2, &g2);
+  if (rc) return rc;
+  bool same23 = (p2 == p3 && n2 == n3);
+  if (!same23) {
+    rc = build_grid(g, p3, n3, &g3);
+    if (rc) return rc;
+  }
+  const Grid& G3 = same23 ? g2 : g3;
+  RppiHist acc;
+  if (variant == 0)
+    count_rppi_literal<P>(R, p1, n1, g2, G3, nthreads, &acc);
+  else
+    count_rppi_lists<P>(R, p1, n1, g2, G3, same23, nthreads, &acc);
+  for (size_t b = 0; b < acc.bins.size(); ++b) hist[b] = acc.bins[b].value();
+  if (overflow) *overflow = acc.overflow.value();
+  return 0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -553,6 +987,133 @@ void oracle_prep_cat_survey(double* c1, long n1, double* c2, long n2, double* bo
   if (c2)
     for (long i = 0; i < n2; ++i)
       for (int d = 0; d < 3; ++d) c2[4 * i + d] -= mn[d];
+}
+
+// Full (rp, pi) histogram of the reference's calculateD1D2D3 for the rppi bin
+// type (source/cudaNcorr.cu:159-216, :220-430 with source/device.cu:317-379
+// or :434-505): nb^3 * nPi^2 doubles in the reference's triCountsAll_ layout
+// (rppi_index above). *overflow receives the total weight of triangles whose
+// index falls past the end of that array, where the reference writes out of
+// bounds. rp_pattern / dot_pattern select the contraction of sqrRpBox and of
+// dotProduct_d3; fma_pattern that of sqrSep. Returns 0, -1 (bad edges, box
+// or nPi), -2 (grid too large), -3 (a point outside the cell grid),
+// -4 (bad args).
+int oracle_count_rppi(const double* box, const double* edges, int n_edges, int num_pi_bins,
+                      int is_survey, const double* ori, const double* p1, long n1, const double* p2,
+                      long n2, const double* p3, long n3, int fma_pattern, int rp_pattern,
+                      int dot_pattern, int nthreads, int variant, double* hist_out, double* overflow) {
+  RppiGeometry R;
+  int rc = make_rppi_geometry(box, edges, n_edges, num_pi_bins, is_survey, ori, &R);
+  if (rc) return rc;
+  const double nbin = std::pow(static_cast<double>(R.g.nb), 3) * R.npi * R.npi;
+  if (nbin + R.npi >= 2147483647.0) return -2;  // the reference indexes with int
+  if (n1 < 0 || n2 < 0 || n3 < 0 || !hist_out) return -4;
+  if (rp_pattern < 0 || rp_pattern > 2 || dot_pattern < 0 || dot_pattern > 5) return -4;
+  R.rp_pat = rp_pattern;
+  R.dot_pat = dot_pattern;
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+  const Pt* a = reinterpret_cast<const Pt*>(p1);
+  const Pt* b = reinterpret_cast<const Pt*>(p2);
+  const Pt* c = reinterpret_cast<const Pt*>(p3);
+  switch (fma_pattern) {
+    case 0: return run_rppi<0>(R, a, n1, b, n2, c, n3, nthreads, variant, hist_out, overflow);
+    case 1: return run_rppi<1>(R, a, n1, b, n2, c, n3, nthreads, variant, hist_out, overflow);
+    case 2: return run_rppi<2>(R, a, n1, b, n2, c, n3, nthreads, variant, hist_out, overflow);
+    case 3: return run_rppi<3>(R, a, n1, b, n2, c, n3, nthreads, variant, hist_out, overflow);
+    case 4: return run_rppi<4>(R, a, n1, b, n2, c, n3, nthreads, variant, hist_out, overflow);
+    case 5: return run_rppi<5>(R, a, n1, b, n2, c, n3, nthreads, variant, hist_out, overflow);
+    default: return -4;
+  }
+}
+
+// getTriangleIndexRppi (source/device.cu:203-255) on three (rp^2, pi^2) sides.
+long oracle_rppi_index(double rp1, double rp2, double rp3, double pi1, double pi2, double pi3,
+                       const double* edges, int n_edges, int num_pi_bins) {
+  std::vector<double> sb(n_edges);
+  for (int i = 0; i < n_edges; ++i) sb[i] = edges[i] * edges[i];
+  return rppi_index(rp1, rp2, rp3, pi1, pi2, pi3, sb, n_edges - 1, num_pi_bins);
+}
+
+// Cell grid of the rppi constructor (source/cudaNcorr.cu:182-193):
+// cell[3] and nc[3]. Returns make_rppi_geometry's status.
+int oracle_rppi_grid(const double* box, const double* edges, int n_edges, int num_pi_bins, int is_survey,
+                     double* cell, int* nc) {
+  RppiGeometry R;
+  int rc = make_rppi_geometry(box, edges, n_edges, num_pi_bins, is_survey, nullptr, &R);
+  if (rc) return rc;
+  for (int d = 0; d < 3; ++d) {
+    cell[d] = R.cellv[d];
+    nc[d] = R.g.nc[d];
+  }
+  return 0;
+}
+
+// prepTriCountsOutRppi (source/cudaNcorr.cu:88-105) and the triBinsOut_ /
+// piBinsOut_ tables of the rppi constructor (source/cudaNcorr.cu:195-213):
+// for every compacted (i <= j <= k, mid[k] <= mid[i] + mid[j]) and every pi
+// pair (l, m): counts, rp mids (3 per entry) and pi bins (l, m) as doubles.
+// Any output may be null; returns the number of entries.
+long oracle_compact_rppi(const double* edges, int n_edges, int num_pi_bins, const double* hist_all,
+                         double* counts_out, double* bins_out, double* pi_out) {
+  const int nb = n_edges - 1;
+  const long P = num_pi_bins;
+  std::vector<double> mid(nb);
+  for (int i = 1; i < n_edges; ++i) mid[i - 1] = (edges[i] + edges[i - 1]) / 2.0;
+  long n = 0;
+  for (int i = 0; i < nb; ++i)
+    for (int j = i; j < nb; ++j)
+      for (int k = j; k < nb; ++k)
+        if (mid[k] <= mid[i] + mid[j])
+          for (long l = 0; l < P; ++l)
+            for (long m = 0; m < P; ++m) {
+              const long idx = m + l * P + k * P * P + j * P * P * nb + static_cast<long>(i) * P * P * nb * nb;
+              if (counts_out) counts_out[n] = hist_all[idx];
+              if (bins_out) {
+                bins_out[3 * n] = mid[i];
+                bins_out[3 * n + 1] = mid[j];
+                bins_out[3 * n + 2] = mid[k];
+              }
+              if (pi_out) {
+                pi_out[2 * n] = static_cast<double>(l);
+                pi_out[2 * n + 1] = static_cast<double>(m);
+              }
+              ++n;
+            }
+  return n;
+}
+
+// The six (rp^2, pi^2) values countTrianglesRppiSurvey derives for the
+// triangle (p1, p2, p3) before its cuts (source/device.cu:446-488):
+// out = {rp1, rp2, rp3, pi1, pi2, pi3}. Used to build inputs that separate
+// the contraction candidates of dotProduct_d3.
+void oracle_survey_rppi_sides(const double* p1, const double* p2, const double* p3, const double* ori,
+                              int fma_pattern, int dot_pattern, double* out) {
+  const Pt& a = *reinterpret_cast<const Pt*>(p1);
+  const Pt& b = *reinterpret_cast<const Pt*>(p2);
+  const Pt& c = *reinterpret_cast<const Pt*>(p3);
+  const double o[3] = {ori[0], 0.0, 0.0};
+  const double A[3] = {a.x - o[0], a.y - o[1], a.z - o[2]};
+  const double B[3] = {b.x - o[0], b.y - o[1], b.z - o[2]};
+  const double C[3] = {c.x - o[0], c.y - o[1], c.z - o[2]};
+  const double los[3] = {A[0] + B[0] + C[0], A[1] + B[1] + C[1], A[2] + B[2] + C[2]};
+  const double sqrL = dot3(dot_pattern, los, los);
+  const Pt* pr[3][2] = {{&a, &b}, {&a, &c}, {&b, &c}};
+  for (int k = 0; k < 3; ++k) {
+    const Pt& u = *pr[k][0];
+    const Pt& v = *pr[k][1];
+    const double d[3] = {u.x - v.x, u.y - v.y, u.z - v.z};
+    const double t = dot3(dot_pattern, los, d);
+    const double pi = (t * t) / sqrL;
+    const double s = oracle_sqr_sep(reinterpret_cast<const double*>(&u), reinterpret_cast<const double*>(&v),
+                                    fma_pattern);
+    out[k] = s - pi;
+    out[3 + k] = pi;
+  }
+}
+
+// sqrRpBox (source/device.cu:38-43) under a given contraction pattern.
+double oracle_sqr_rp(const double* a, const double* b, int rp_pattern) {
+  return rp_sum(rp_pattern, a[0] - b[0], a[1] - b[1]);
 }
 
 }  // extern "C"

@@ -160,3 +160,167 @@ def fma_probe(seed=17, n_clusters=48):
         cpt = np.append(m + np.sqrt(16.0 ** 2 - (e / 2.0) ** 2) * v, 1.0)
         rows += [a, b, cpt]
     return dict(box=240.0, edges=edges, p=np.array(rows), survey=False)
+
+
+# ------------------------------------------------------------------ rppi (rp, pi) bin type
+RPPI_EDGES = np.array([0.0, 5.0, 10.0, 15.0, 20.0])  # nb = 4, rpMax = 20
+RPPI_NPI = 10  # unit pi bins 0..10, piMax = 10; box cells (20, 20, 10)
+
+
+def rppi_flat(ip2, ip1, i3, i2, i1, nb=4, npi=RPPI_NPI):
+    """getTriangleIndexRppi's flat index (source/device.cu:251)."""
+    return ip2 + ip1 * npi + i3 * npi * npi + i2 * nb * npi * npi + i1 * nb * nb * npi * npi
+
+
+def rppi_kat_tie():
+    """Sides AB (rp^2 25, pi^2 4), AC (64, 1), BC (25, 1). AB and BC tie on
+    rp^2, so the pi bins of the two shortest sides follow the reference's
+    swap order: anchors A (both orders) and B (A then C) give pi bins (2, 1),
+    the other three orderings (1, 2)."""
+    p = pts((50, 50, 50), (53, 54, 52), (50, 58, 51))
+    expect = {rppi_flat(1, 2, 1, 1, 1): 3.0, rppi_flat(2, 1, 1, 1, 1): 3.0}
+    return dict(box=100.0, edges=RPPI_EDGES, npi=RPPI_NPI, p=p, expect=expect, overflow=0.0, survey=False)
+
+
+def rppi_kat_pi_cut():
+    """AB has pi^2 = 100 = piMax^2 exactly: pi^2 < piMax^2 is strict, so no
+    ordering of ABC counts, although AC and BC are in range."""
+    p = pts((50, 50, 45), (53, 54, 55), (50, 58, 50))
+    return dict(box=100.0, edges=RPPI_EDGES, npi=RPPI_NPI, p=p, expect={}, overflow=0.0, survey=False)
+
+
+def rppi_kat_pi_overflow():
+    """AB has pi^2 = (10 - 2^-30)^2 < 100, whose FP32 square root rounds to
+    10 = nPi. All sides fall in the last rp bin and AB sorts second, so every
+    ordering's index is nb^3 * nPi^2: one past the histogram, where the
+    reference writes out of bounds. All six go to the overflow counter."""
+    t = np.deg2rad(70.0)
+    p = pts((50.0, 50.0, 40.0), (66.0, 50.0, 50.0 - 2.0 ** -30),
+            (50.0 + 15.5 * np.cos(t), 50.0 + 15.5 * np.sin(t), 49.5))
+    return dict(box=100.0, edges=RPPI_EDGES, npi=RPPI_NPI, p=p, expect={}, overflow=6.0, survey=False)
+
+
+RPPI_KATS = [rppi_kat_tie, rppi_kat_pi_cut, rppi_kat_pi_overflow]
+
+
+def rppi_expected_hist(case):
+    nb = len(case["edges"]) - 1
+    h = np.zeros(nb ** 3 * case["npi"] ** 2)
+    for k, v in case["expect"].items():
+        h[k] = v
+    return h
+
+
+def rppi_small_box(seed=21, n=2500, box=200.0):
+    """Uniform box, L = 200, rp edges 0..25 in 5 bins, 15 pi bins
+    (cells 25 x 25 x 15: 8 x 8 x 14)."""
+    return C.uniform_box(n, box, seed), box, C.linear_edges(25.0, 5), 15
+
+
+def rppi_small_box_clustered(seed=22):
+    """Neyman-Scott, L = 300, rp 12 log bins in [1, 30), 20 pi bins; the last
+    z cell is 20 wide of 20 (divisible) and x cells 30 (divisible)."""
+    from oracle import oracle as O
+    return C.neyman_scott(300, 8.0, 2.0, 300.0, seed), 300.0, O.logspace(1.0, 30.0, 13), 20
+
+
+def rppi_small_box_nondivisible(seed=23):
+    """L = 100, rpMax = 30 (4 cells, the last 10 wide), 12 pi bins (9 cells,
+    the last 4 wide)."""
+    return C.uniform_box(1200, 100.0, seed), 100.0, C.linear_edges(30.0, 6), 12
+
+
+def rppi_small_survey(seed=24, nd=1500, nr=3000, weighted=False):
+    """Survey wedge scaled down, jointly shifted; rp 8 log bins in [2, 30),
+    20 pi bins (cells of sqrtf(30^2 + 20^2))."""
+    from oracle import oracle as O
+    d = C.survey_wedge(nd, seed, weighted, ra_max_deg=12.0, dec_max_deg=10.0)
+    r = C.survey_wedge(nr, seed + 1000, False, ra_max_deg=12.0, dec_max_deg=10.0)
+    box, ori = O.prep_cat_survey(d, r)
+    return d, r, box, ori, O.logspace(2.0, 30.0, 9), 20
+
+
+def _probe_edges(n_clusters):
+    """Inner edges 1..4 (two per cluster plus one), rpMax 6: small enough a
+    histogram with 5 pi bins (nb^3 * 25 entries) for the oracle."""
+    n_inner = 2 * n_clusters + 1
+    return np.array([0.0] + list(np.linspace(1.0, 4.0, n_inner)) + [6.0])
+
+
+def rppi_box_probe(seed=25, n_clusters=12):
+    """Isolated box triangles whose side AB has rp^2 within a few ulps of a
+    bin edge, chosen so that the three contraction candidates of sqrRpBox
+    disagree on its bin (as fma_probe does for sqrSep). 5 pi bins; clusters
+    60 apart in a 240 box (cells 6 x 6 x 5)."""
+    from oracle import oracle as O
+    rng = np.random.default_rng(seed)
+    edges = _probe_edges(n_clusters)
+    rows = []
+    centres = [(30.0 + 60.0 * i, 30.0 + 60.0 * j, 30.0 + 60.0 * k)
+               for i in range(4) for j in range(4) for k in range(3)][:n_clusters]
+    for ci, c in enumerate(centres):
+        e = edges[2 * ci + 2]
+        target = e * e
+        for _ in range(200000):
+            a = np.array([c[0] + rng.random(), c[1] + rng.random(), c[2] + rng.random(), 1.0])
+            phi = rng.random() * 2 * np.pi
+            u = np.array([np.cos(phi), np.sin(phi), 0.0])
+            b = a.copy()
+            b[:3] = a[:3] + e * u
+            b[2] = a[2] + rng.uniform(0.2, 0.9)
+            if len({O.sqr_rp(a, b, k) >= target for k in range(3)}) > 1:
+                break
+        else:
+            raise RuntimeError("no distinguishing pair found")
+        v = np.array([-u[1], u[0], 0.0])
+        m = (a[:3] + b[:3]) / 2.0
+        cpt = np.append(m + np.sqrt(4.5 ** 2 - (e / 2.0) ** 2) * v + np.array([0.0, 0.0, 0.3]), 1.0)
+        rows += [a, b, cpt]
+    return dict(box=240.0, edges=edges, npi=5, p=np.array(rows), survey=False, ori=(0.0, 0.0, 0.0))
+
+
+def rppi_survey_probe(seed=27, n_clusters=12):
+    """Isolated survey triangles whose side AB has rp^2 = s^2 - pi^2 within a
+    few ulps of a bin edge with pi^2 of the same size, chosen so that the six
+    contraction candidates of dotProduct_d3 disagree on its bin. B is placed
+    at A + e*u + p*n with u perpendicular to the line of sight n, so
+    rp^2 ~ e^2 and pi^2 ~ p^2; n is re-derived from the final positions.
+    5 pi bins, clusters 60 apart in a 240 box, ori.x = -700."""
+    from oracle import oracle as O
+    rng = np.random.default_rng(seed)
+    edges = _probe_edges(n_clusters)
+    ori = np.array([-700.0, -800.0, -900.0])
+    rows = []
+    centres = [(30.0 + 60.0 * i, 30.0 + 60.0 * j, 30.0 + 60.0 * k)
+               for i in range(4) for j in range(4) for k in range(3)][:n_clusters]
+    off = np.array([ori[0], 0.0, 0.0])
+    for ci, c in enumerate(centres):
+        e = edges[2 * ci + 2]
+        target = e * e
+        found = False
+        for _ in range(20000):
+            a = np.array([c[0] + rng.random(), c[1] + rng.random(), c[2] + rng.random(), 1.0])
+            cpt = a.copy()
+            cpt[:3] = a[:3] + rng.normal(size=3) * 1.5
+            p = e * rng.uniform(0.8, 1.2)
+            b = a.copy()
+            u = None
+            for _ in range(12):  # the line of sight moves with B: iterate to a fixed point
+                los = (a[:3] - off) + (b[:3] - off) + (cpt[:3] - off)
+                n = los / np.linalg.norm(los)
+                if u is None:
+                    u = np.cross(n, rng.normal(size=3))
+                u = u - np.dot(u, n) * n
+                u /= np.linalg.norm(u)
+                b[:3] = a[:3] + e * u + p * n
+            sides = [O.survey_rppi_sides(a, b, cpt, ori, dot_pattern=k) for k in range(6)]
+            if len({s[0] >= target for s in sides}) > 1:
+                s = sides[O.DOT_PATTERN]
+                if all(0.0 < s[i] < 36.0 for i in range(3)) and all(s[3 + i] < 25.0 for i in range(3)):
+                    found = True
+                    break
+        if not found:
+            raise RuntimeError("no distinguishing triangle found")
+        rows += [a, b, cpt]
+    return dict(box=np.array([240.0, 240.0, 240.0]), edges=edges, npi=5, p=np.array(rows), survey=True,
+                ori=tuple(ori))

@@ -35,10 +35,25 @@ def test_bad_bin_type_is_rejected(engine_lib):
     assert e.value.code in (api.NCORR_ERR_INVALID_ARGUMENT, api.NCORR_ERR_NO_DEVICE)
 
 
-def test_rppi_is_not_implemented(engine_lib):
+def test_rppi_constructor_checks_its_arguments(engine_lib):
+    """The rppi constructor rejects another bin type (the reference throws)
+    and a pi binning with no bins, before it looks for a device."""
     with pytest.raises(api.NcorrError) as e:
-        api.ncorr((100.0, 100.0, 100.0), api.rppi, [0.0, 5.0, 10.0], False, (0, 0, 0), numMinorBins=4)
-    assert e.value.code == api.NCORR_ERR_NOT_IMPLEMENTED
+        api.ncorr((100.0, 100.0, 100.0), api.threeD, [0.0, 5.0, 10.0], 4, False, (0, 0, 0))
+    assert e.value.code == api.NCORR_ERR_INVALID_ARGUMENT
+    for bad in (0, -3):
+        with pytest.raises(api.NcorrError) as e:
+            api.ncorr((100.0, 100.0, 100.0), api.rppi, [0.0, 5.0, 10.0], bad, False, (0, 0, 0))
+        assert e.value.code == api.NCORR_ERR_INVALID_ARGUMENT
+
+
+def test_smu_is_rejected_by_both_constructors(engine_lib):
+    """smu is declared by the reference (include/cudaNcorr.hpp:12) but both
+    of its constructors throw for it."""
+    for args in ((False, (0, 0, 0)), (4, False, (0, 0, 0))):
+        with pytest.raises(api.NcorrError) as e:
+            api.ncorr((100.0, 100.0, 100.0), api.smu, [0.0, 5.0, 10.0], *args)
+        assert e.value.code == api.NCORR_ERR_INVALID_ARGUMENT
 
 
 @pytest.mark.parametrize("edges", [[5.0], [0.0, 5.0, 5.0], [-1.0, 5.0], [0.0, float("nan")]])

@@ -122,7 +122,7 @@ def test_fma_patterns_differ_on_adversarial_pairs(oracle):
 
 
 def _golden_files():
-    return sorted(GOLDEN.glob("*.json"))
+    return sorted(p for p in GOLDEN.glob("*.json") if not p.name.startswith("rppi_"))
 
 
 @pytest.mark.parametrize("path", _golden_files(), ids=lambda p: p.stem)
