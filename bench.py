@@ -44,6 +44,9 @@ METRIC = "triangles/sec"
 UNIT = "triangles/s"
 N_SM = 152
 FP32_LANES_PER_SM = 128
+# FP64 FMA throughput of this machine's GB300, measured with a DFMA loop
+# (1.20 TFLOP/s, 1/63 of the FP32 rate); the rppi kernel's denominator.
+FP64_PEAK_TFLOPS = 1.20
 L2_FLUSH_BYTES = 256 << 20
 # Triangle-kernel DRAM traffic per launch (dram__bytes_read.sum +
 # dram__bytes_write.sum): 27.37 MB measured with ncu on the 249,814-point
@@ -618,6 +621,158 @@ def run_survey(args) -> dict:
     return out if rank == 0 else None
 
 
+RPPI_NPI = 30
+
+
+def rppi_workload(seed_offset: int, logspace):
+    """The clustered box of the default workload with the rppi binning: rp in
+    12 log bins on [1, 30) Mpc/h, 30 unit pi bins (piMax = 30 Mpc/h), line of
+    sight z. The reference quotes no rppi configuration; this is a typical
+    projected 3PCF binning."""
+    from cudancorr_gb300 import catalogs as C
+    p, box, _ = C.config_box_clustered(seed=2 + seed_offset)
+    edges = logspace(1.0, 30.0, 13)
+    desc = ("Neyman-Scott box: 200,000 parents x Poisson(10), sigma 2, L=2000 Mpc/h; rppi: rp 12 log bins "
+            "in [1,30), 30 unit pi bins, unweighted")
+    return p, box, edges, RPPI_NPI, desc
+
+
+def run_rppi(args) -> dict:
+    """The rppi bin type (the reference's second constructor) on one GPU."""
+    import torch
+    from cudancorr_gb300 import api
+
+    world, rank, local = dist_setup()
+    p, box, edges, npi, desc = rppi_workload(rank, api.logspace)
+    dev = torch.device("cuda", local)
+    t_cat = torch.from_numpy(p).to(dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    corr = api.ncorr(np.full(3, box), api.rppi, edges, npi, False, (0.0, 0.0, 0.0))
+
+    def device_step():
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        corr._calculate_device(t_cat, t_cat, t_cat, stream=stream.cuda_stream)
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1), corr.stats()
+
+    for _ in range(args.warmup):
+        device_step()
+    sampler = ClockSampler(local)
+    sampler.start()
+    barrier(world)
+    step_ms, kernel_ms, tri = [], [], []
+    for _ in range(args.steps):
+        ms, st = device_step()
+        step_ms.append(ms)
+        kernel_ms.append(st["ms_count"])
+        tri.append(st["triangles"])
+    barrier(world)
+    clocks = sampler.stop()
+    st_last = corr.stats()
+    total_ms = barrier_max(sum(step_ms), world)
+    total_tri = barrier_sum(float(sum(tri)), world)
+    p_host = torch.from_numpy(p).pin_memory().numpy()
+    corr.calculateD1D2D3(p_host, p_host, p_host)
+    barrier(world)
+    e2e_ms = []
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        corr.calculateD1D2D3(p_host, p_host, p_host)
+        _ = corr.getTriCountsOut()
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    e2e_total = barrier_max(sum(e2e_ms), world)
+    n_out = len(corr.getTriCountsOut())
+    corr.close()
+    # FP64 roofline: each candidate pair that passes the FP32 prefilter is
+    # evaluated in FP64 -- dz, dz^2, dx, dy, dy^2, fma(dx, dx, .) -- 7 flops
+    # (the fma counts 2) before its cuts and index.
+    fp64_flops = 7.0 * st_last["n_exact_tris"]
+    achieved = fp64_flops / (statistics.mean(kernel_ms) / 1e3) / 1e12
+    nb = len(edges) - 1
+    out = {
+        "metric": METRIC, "value": total_tri / (total_ms / 1e3), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp64 (fp32 prefilter)",
+        "data": "synthetic (seeded)",
+        "config": {"workload": "rppi_box_clustered", "description": desc, "n_points": int(len(p)), "box": box,
+                   "rp_max": float(edges[-1]), "rp_bins": nb, "pi_bins": npi, "triangles_per_step": int(tri[-1]),
+                   "overflow_per_step": float(st_last["overflow"]),
+                   "l2": "flushed (256 MiB write) between steps",
+                   "parallelism": f"{world} independent catalogue(s), one per GPU"},
+        "e2e": {"value": total_tri / (e2e_total / 1e3), "unit": UNIT, "h2d_bytes_per_step": int(p.nbytes),
+                "d2h_bytes_per_step": int(nb ** 3 * npi * npi * 8), "ms_per_step": e2e_total / args.steps},
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
+                     "frac": achieved / FP64_PEAK_TFLOPS, "traffic": None, "kernel": "k_rppi",
+                     "kernel_ms": statistics.mean(kernel_ms),
+                     "work": "7 FP64 flops x pairs evaluated in FP64 (past the FP32 prefilter)",
+                     "pairs_visited": int(st_last["n_pairs"]), "pairs_fp64": int(st_last["n_exact_tris"]),
+                     "peak_basis": "DFMA loop measured on this pool's GB300 (MEASURED_PEAKS.json has no FP64 entry)"},
+        "gpu_launches": 4 * args.steps,
+        "clocks": clocks,
+        "n_out": n_out,
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        from oracle import oracle as O
+        threads = os.cpu_count() or 1
+        rng = np.random.default_rng(7)
+        n = 4096
+        sub = np.ascontiguousarray(p[rng.choice(len(p), n, replace=False)])
+        t = time.perf_counter()
+        h, _ = O.count_rppi(box, edges, npi, sub, p, p, nthreads=threads)
+        dt = time.perf_counter() - t
+        n2 = int(min(len(p), n * 10.0 / max(dt, 1e-3)))
+        sub = np.ascontiguousarray(p[rng.choice(len(p), n2, replace=False)])
+        t = time.perf_counter()
+        h, _ = O.count_rppi(box, edges, npi, sub, p, p, nthreads=threads)
+        dt = time.perf_counter() - t
+        out["cpu_baseline"] = {"value": float(h.sum() / dt), "unit": UNIT, "cores": threads, "kind": "port",
+                               "sample": f"{n2} random anchors of the {len(p):,}-point catalogue, {dt:.1f} s, "
+                                         "oracle/ncorr_oracle.cpp rppi neighbour-list form"}
+    return out if rank == 0 else None
+
+
+def run_reference_rppi(args) -> dict:
+    """The reference's own rppi kernel (countTrianglesRppiBox from the
+    oracle/_ref cubin) behind its host flow, on a random anchor sample."""
+    from oracle import oracle as O
+    p, box, edges, npi, desc = rppi_workload(0, O.logspace)
+    for _ in range(args.warmup):
+        O.reference_count_rppi(box, edges, npi, p[:2048], p, p)
+    rng = np.random.default_rng(11)
+    n_sub = min(len(p), args.ref_anchors)
+    tri, tot_ms, k_ms = [], [], []
+    for _ in range(args.steps):
+        sub = np.ascontiguousarray(p[rng.choice(len(p), n_sub, replace=False)])
+        h, ov, kms, tms = O.reference_count_rppi(box, edges, npi, sub, p, p)
+        tri.append(h.sum() + ov)
+        tot_ms.append(tms)
+        k_ms.append(kms)
+    value = sum(tri) / (sum(tot_ms) / 1e3)
+    sample = (f"{n_sub} random anchors per timed step of the {len(p):,}-point catalogue; reference "
+              f"source/device.cu countTrianglesRppiBox, unmodified, on the GB300 via oracle/ref_runner.cu")
+    return {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": sum(tot_ms) / len(tot_ms),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
+        "data": "synthetic (seeded)",
+        "config": {"workload": "rppi_box_clustered", "description": desc, "n_points": int(len(p)),
+                   "anchor_sample": n_sub, "l2": "inputs staged per call by the reference host flow"},
+        "kernel_only": {"value": sum(tri) / (sum(k_ms) / 1e3), "unit": UNIT, "ms_per_step": sum(k_ms) / len(k_ms)},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "reference",
+                         "device": "GB300 (the reference's CUDA kernel; one host thread drives it)",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
 def run_reference(args) -> dict:
     """The reference's own kernel (oracle/_ref cubin, compiled unmodified from
     its source/device.cu) behind a restatement of its host flow, on a random
@@ -639,6 +794,8 @@ def run_reference(args) -> dict:
         O.runner()
     except Exception as e:  # the cubin is built where the reference sources are mounted
         return {"impl": "reference", "unavailable": f"reference kernel not loadable: {e}"}
+    if args.workload == "rppi_box_clustered":
+        return run_reference_rppi(args)
     if args.workload in ("batch_mocks", "survey"):
         return {"impl": "reference", "unavailable": "the reference arm times the single-catalogue box workloads; "
                                                     f"{args.workload} would take the reference kernel hours"}
@@ -685,7 +842,7 @@ def main():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--workload", default="box_clustered",
                     choices=["box_clustered", "box_clustered_L1000", "box_uniform", "soneira_peebles",
-                             "batch_mocks", "survey"])
+                             "batch_mocks", "survey", "rppi_box_clustered"])
     ap.add_argument("--schedule", default="dynamic", choices=["dynamic", "static", "learned"],
                     help="anchor order of the triangle kernel (learned: trains the work model first)")
     ap.add_argument("--no-autotune", action="store_true", help="batch_mocks: default tuning")
@@ -703,6 +860,8 @@ def main():
         out = run_batch(args)
     elif args.workload == "survey":
         out = run_survey(args)
+    elif args.workload == "rppi_box_clustered":
+        out = run_rppi(args)
     else:
         out = run_engine(args)
     if out is not None:

@@ -54,9 +54,11 @@ struct Geom {
   float ka, kb;
   // Prefilter of the pair stage on cell-local FP32 estimates.
   float pre_lo, pre_hi;
-  // Heron margin: a candidate triangle is certainly accepted by the
-  // reference's FP32 sqrtf test when H > S*(ha*S + hb), S = a+b+c.
-  float ha, hb;
+  // Triangle-test margin: with list values rho_j, rho_l (square roots of the
+  // r1^2 and r2^2 estimates) and third side v, the reference's FP32 sqrtf
+  // test certainly keeps the triangle when
+  // |v - (rho_j^2 + rho_l^2)| < 2 rho_j rho_l + hm  (hm = -M < 0).
+  float hm;
   // Bin table: code of r^2 = table[rint(v*tab_scale)], clamped to the last entry.
   float tab_scale;
   int tab_n;

@@ -198,11 +198,19 @@ inline float f32_up(double x) {
 //  * The prefilter estimate from cell-local coordinates (error <= 5u*cell +
 //    u|D| per component) satisfies |v - V| <= 14u V + 9u r_max^2; only used
 //    to skip candidates that are certainly out of range (pa, pb).
-//  * Heron: with |x - X| <= ka x + kb for all three sides, the exact Heron
-//    product H = 4ab - (c-a-b)^2 moves by <= 2S(ka S + 3 kb), its FP32
-//    evaluation errs by <= 6u S^2, and H >= 8.3u c_max^2 proves that the
-//    reference's FP32 sqrtf test keeps the triangle. Hence the test
-//    H > S (ha S + hb).
+//  * Triangle test. Let A, B, C be the reference's r^2 of the sides
+//    anchor-j, anchor-l, j-l, all below r_max^2 for a candidate that can
+//    count, and Q = 2 sqrt(AB) - |C - A - B|. The sorted quantity
+//    (p + q)^2 - r^2 of the reference's test (p <= q <= r the square roots)
+//    is >= Q whichever side is longest, and the FP32 test sqrtf(x1) +
+//    sqrtf(x2) > sqrtf(x3) errs by at most 6.5u r_max in p + q - r; so
+//    Q > 19.8u r_max^2 proves the triangle is kept. The list stores
+//    rho = sqrt_rn(a) with a within 5.1u A, so rho^2 is within 7.2u A and
+//    2 rho_j rho_l within 7.2u of 2 sqrt(AB). The kernel evaluates
+//    t = v - fma(rho_l, rho_l, rho_j^2) (error <= 30.7u r_max^2, with the
+//    7u V + 2u r_max^2 bound on v) and w = fma(2 rho_j, rho_l, -M) (error
+//    <= 16.5u r_max^2), and keeps the candidate when |t| < w: then
+//    Q > M - 47.2u r_max^2. M = 128u r_max^2 leaves a factor of two.
 // Margins are generous on purpose: a wider band only sends more candidates
 // to the exact FP64 path.
 inline void set_error_model(Geom& g) {
@@ -210,8 +218,7 @@ inline void set_error_model(Geom& g) {
   const double r2 = g.sqr_rmax;
   g.ka = static_cast<float>(12.0 * u);
   g.kb = static_cast<float>(4.0 * u * r2);
-  g.ha = static_cast<float>(48.0 * u);
-  g.hb = static_cast<float>(32.0 * u * r2);
+  g.hm = -f32_up(128.0 * u * r2);
   // Prefilter thresholds: candidates with v >= pre_hi or v <= pre_lo are
   // certainly outside (r_min^2, r_max^2).
   const double eb = 20.0 * u, ec = 12.0 * u * r2;

@@ -16,14 +16,14 @@
 //           (rigorous error band; the rare undecided ones are recomputed in
 //           FP64 exactly as the reference computes them). In-range neighbours
 //           go to a list in shared memory (overflow: a per-CTA global slab):
-//           offset d (float3), r1^2 estimate, exact bin, slot, point index,
-//           weight.
+//           offset d (float3), the square root of the r1^2 estimate, exact
+//           bin, slot, point index, weight.
 //  Phase B  every neighbour pair (j, l) of the list(s) is a candidate
 //           triangle. Work items are (l-tile of 128 entries, 32 j-entries);
 //           warps take items from a shared counter. A warp holds its l-tile in
 //           registers (4 per lane) and streams the j-entries as warp-wide
 //           broadcasts. Per candidate: |d_j - d_l|^2 in FP32, its bin from a
-//           shared-memory table, a Heron test proving the reference's FP32
+//           shared-memory table, a margin test proving the reference's FP32
 //           triangle test, and one predicated shared atomic into the CTA's
 //           (bin_j, bin_l, bin_3) histogram. Candidates whose FP32
 //           classification is not certain are queued per warp and settled by
@@ -176,6 +176,18 @@ struct ListView {
   __device__ __forceinline__ float W(int i, int ks) const { return i < ks ? w[i] : sw[i - ks]; }
 };
 
+// The margin form of the triangle test. List entries keep rho = sqrt_rn of
+// their r^2 estimate in .w; with a = rho_j^2 and b = rho_l^2 (the products
+// formed inside the FMAs) a candidate of third side v is certainly kept by
+// the reference's FP32 sqrtf test when |v - (a + b)| < 2 rho_j rho_l - M
+// (hm = -M; the PTX body evaluates the same operations).
+__device__ __forceinline__ bool heron_clean(float v, float aj, float a2r, float rl, float hm) {
+  const float s = fmaf(rl, rl, aj);
+  const float t = __fsub_rn(v, s);
+  const float w = fmaf(a2r, rl, hm);
+  return fabsf(t) < w;
+}
+
 // Signed 128-bit accumulate into (lo, hi) words of global memory.
 __device__ __forceinline__ void add128(unsigned long long* w, long long v) {
   const unsigned long long lo = static_cast<unsigned long long>(v);
@@ -231,15 +243,11 @@ __device__ __forceinline__ void red_shared_u64_if(unsigned addr, unsigned long l
   "add.u32 ia, ia, %14;\n\t"                   \
   "min.u32 ia, ia, %15;\n\t"                   \
   "ld.shared.u8 code, [ia];\n\t"               \
-  "add.rn.f32 s, %4, %9;\n\t"                  \
+  "fma.rn.f32 s, %9, %9, %4;\n\t"              \
   "sub.rn.f32 t, v, s;\n\t"                    \
-  "neg.f32 nt, t;\n\t"                         \
-  "mul.rn.f32 p4, %5, %9;\n\t"                 \
-  "fma.rn.f32 H, nt, t, p4;\n\t"               \
-  "add.rn.f32 S, s, v;\n\t"                    \
-  "fma.rn.f32 qq, %17, S, %18;\n\t"            \
-  "mul.rn.f32 nd, S, qq;\n\t"                  \
-  "setp.gt.f32 cl, H, nd;\n\t"                 \
+  "abs.f32 t, t;\n\t"                          \
+  "fma.rn.f32 H, %5, %9, %17;\n\t"             \
+  "setp.lt.f32 cl, t, H;\n\t"                  \
   "setp.lt.u32 ok, code, %16;\n\t"             \
   "setp.eq.u32 car, code, 255;\n\t"            \
   NCORR_CAND_MASK                              \
@@ -256,7 +264,7 @@ __device__ __forceinline__ void red_shared_u64_if(unsigned addr, unsigned long l
   "and.pred car, car, inp;\n\t"
 
 #define NCORR_CAND_DECLS                                         \
-  ".reg .f32 dx, dy, dz, v, y, s, t, nt, p4, H, S, qq, nd;\n\t" \
+  ".reg .f32 dx, dy, dz, v, y, s, t, H;\n\t"                   \
   ".reg .b32 ia, code, key, adr;\n\t"                            \
   ".reg .pred ok, cl, ncl, car, upd, wq, inp;\n\t"
 
@@ -269,23 +277,22 @@ __device__ __forceinline__ void red_shared_u64_if(unsigned addr, unsigned long l
 // adds to the lane's own scratch word `dummy` instead, which keeps the loop
 // free of the branch a predicated atomic compiles to.
 template <bool DIAG>
-__device__ __forceinline__ unsigned cand_count(float ex, float ey, float ez, float a, float a4, float lx,
+__device__ __forceinline__ unsigned cand_count(float ex, float ey, float ez, float a, float a2r, float lx,
                                                float ly, float lz, float b, unsigned kj, unsigned kl,
                                                unsigned in, float tscale, unsigned tab_adj,
-                                               unsigned tab_last, unsigned nb_cs, float ha, float hb,
-                                               unsigned dummy) {
+                                               unsigned tab_last, unsigned nb_cs, float hm, unsigned dummy) {
   unsigned q;
 #define NCORR_CAND_COUNT_ASM                                                                          \
   asm volatile(                                                                                      \
       "{\n\t" NCORR_CAND_DECLS NCORR_CAND_CLASSIFY                                                     \
       "add.u32 key, %10, %11;\n\t"                                                                   \
       "add.u32 key, key, code;\n\t"                                                                  \
-      "selp.b32 adr, key, %19, upd;\n\t"                                                             \
+      "selp.b32 adr, key, %18, upd;\n\t"                                                             \
       "red.shared.add.u32 [adr], 1;\n\t"                                                             \
       "}"                                                                                            \
       : "=r"(q)                                                                                      \
-      : "f"(ex), "f"(ey), "f"(ez), "f"(a), "f"(a4), "f"(lx), "f"(ly), "f"(lz), "f"(b), "r"(kj), "r"(kl), \
-        "r"(in), "f"(tscale), "r"(tab_adj), "r"(tab_last), "r"(nb_cs), "f"(ha), "f"(hb), "r"(dummy))
+      : "f"(ex), "f"(ey), "f"(ez), "f"(a), "f"(a2r), "f"(lx), "f"(ly), "f"(lz), "f"(b), "r"(kj), "r"(kl), \
+        "r"(in), "f"(tscale), "r"(tab_adj), "r"(tab_last), "r"(nb_cs), "f"(hm), "r"(dummy))
   if (DIAG) {
 #define NCORR_CAND_MASK NCORR_CAND_MASK_ON
     NCORR_CAND_COUNT_ASM;
@@ -310,11 +317,10 @@ __device__ __forceinline__ unsigned cand_count(float ex, float ey, float ez, flo
 // thread's carry comes from its own atomic on the low word, so the 64-bit
 // total is exact however the adds interleave.
 template <bool DIAG>
-__device__ __forceinline__ unsigned cand_wsum(float ex, float ey, float ez, float a, float a4, float lx,
+__device__ __forceinline__ unsigned cand_wsum(float ex, float ey, float ez, float a, float a2r, float lx,
                                               float ly, float lz, float b, unsigned kj, unsigned kl,
                                               unsigned in, float tscale, unsigned tab_adj, unsigned tab_last,
-                                              unsigned nb_cs, float ha, float hb, unsigned dummy, float wrow,
-                                              float wl) {
+                                              unsigned nb_cs, float hm, unsigned dummy, float wrow, float wl) {
   unsigned q;
 #define NCORR_CAND_WSUM_ASM                                                                           \
   asm volatile(                                                                                      \
@@ -322,8 +328,8 @@ __device__ __forceinline__ unsigned cand_wsum(float ex, float ey, float ez, floa
       ".reg .f32 wp;\n\t.reg .b32 wi, whi, wold, wnew, wcy, adrh;\n\t" NCORR_CAND_CLASSIFY              \
       "add.u32 key, %10, %11;\n\t"                                                                   \
       "add.u32 key, key, code;\n\t"                                                                  \
-      "selp.b32 adr, key, %19, upd;\n\t"                                                             \
-      "mul.rn.f32 wp, %20, %21;\n\t"                                                                 \
+      "selp.b32 adr, key, %18, upd;\n\t"                                                             \
+      "mul.rn.f32 wp, %19, %20;\n\t"                                                                 \
       "cvt.rni.s32.f32 wi, wp;\n\t"                                                                  \
       "shr.s32 whi, wi, 31;\n\t"                                                                     \
       "atom.shared.add.u32 wold, [adr], wi;\n\t"                                                     \
@@ -334,8 +340,8 @@ __device__ __forceinline__ unsigned cand_wsum(float ex, float ey, float ez, floa
       "red.shared.add.u32 [adrh], whi;\n\t"                                                          \
       "}"                                                                                            \
       : "=r"(q)                                                                                      \
-      : "f"(ex), "f"(ey), "f"(ez), "f"(a), "f"(a4), "f"(lx), "f"(ly), "f"(lz), "f"(b), "r"(kj), "r"(kl), \
-        "r"(in), "f"(tscale), "r"(tab_adj), "r"(tab_last), "r"(nb_cs), "f"(ha), "f"(hb), "r"(dummy),   \
+      : "f"(ex), "f"(ey), "f"(ez), "f"(a), "f"(a2r), "f"(lx), "f"(ly), "f"(lz), "f"(b), "r"(kj), "r"(kl), \
+        "r"(in), "f"(tscale), "r"(tab_adj), "r"(tab_last), "r"(nb_cs), "f"(hm), "r"(dummy),           \
         "f"(wrow), "f"(wl))
   if (DIAG) {
 #define NCORR_CAND_MASK NCORR_CAND_MASK_ON
@@ -352,31 +358,28 @@ __device__ __forceinline__ unsigned cand_wsum(float ex, float ey, float ez, floa
 
 // Counting body of the shared-histogram path: count or weighted sum.
 template <bool WEIGHTED, bool DIAG>
-__device__ __forceinline__ unsigned cand_body(float ex, float ey, float ez, float a, float a4, float lx,
+__device__ __forceinline__ unsigned cand_body(float ex, float ey, float ez, float a, float a2r, float lx,
                                               float ly, float lz, float b, unsigned kj, unsigned kl,
                                               unsigned in, float tscale, unsigned tab_adj, unsigned tab_last,
-                                              unsigned nb_cs, float ha, float hb, unsigned dummy, float wrow,
-                                              float wl) {
+                                              unsigned nb_cs, float hm, unsigned dummy, float wrow, float wl) {
   if (WEIGHTED)
-    return cand_wsum<DIAG>(ex, ey, ez, a, a4, lx, ly, lz, b, kj, kl, in, tscale, tab_adj, tab_last, nb_cs, ha, hb,
+    return cand_wsum<DIAG>(ex, ey, ez, a, a2r, lx, ly, lz, b, kj, kl, in, tscale, tab_adj, tab_last, nb_cs, hm,
                            dummy, wrow, wl);
-  return cand_count<DIAG>(ex, ey, ez, a, a4, lx, ly, lz, b, kj, kl, in, tscale, tab_adj, tab_last, nb_cs, ha, hb,
-                          dummy);
+  return cand_count<DIAG>(ex, ey, ez, a, a2r, lx, ly, lz, b, kj, kl, in, tscale, tab_adj, tab_last, nb_cs, hm, dummy);
 }
 
 // The same classification without the histogram update: 1 when the
 // candidate needs the careful/exact path.
-__device__ __forceinline__ unsigned cand_flag(float ex, float ey, float ez, float a, float a4, float lx,
+__device__ __forceinline__ unsigned cand_flag(float ex, float ey, float ez, float a, float a2r, float lx,
                                               float ly, float lz, float b, unsigned in, float tscale,
-                                              unsigned tab_adj, unsigned tab_last, unsigned nb_cs, float ha,
-                                              float hb) {
+                                              unsigned tab_adj, unsigned tab_last, unsigned nb_cs, float hm) {
   unsigned q;
 #define NCORR_CAND_MASK NCORR_CAND_MASK_ON
   asm volatile(
       "{\n\t" NCORR_CAND_DECLS NCORR_CAND_CLASSIFY "}"
       : "=r"(q)
-      : "f"(ex), "f"(ey), "f"(ez), "f"(a), "f"(a4), "f"(lx), "f"(ly), "f"(lz), "f"(b), "r"(0u), "r"(0u),
-        "r"(in), "f"(tscale), "r"(tab_adj), "r"(tab_last), "r"(nb_cs), "f"(ha), "f"(hb));
+      : "f"(ex), "f"(ey), "f"(ez), "f"(a), "f"(a2r), "f"(lx), "f"(ly), "f"(lz), "f"(b), "r"(0u), "r"(0u),
+        "r"(in), "f"(tscale), "r"(tab_adj), "r"(tab_last), "r"(nb_cs), "f"(hm));
 #undef NCORR_CAND_MASK
   return q;
 }
@@ -532,10 +535,7 @@ __device__ __noinline__ void cold_drain(Cold& c) {
       const unsigned key_jl = ((mj & 0xffu) * nb * nb + (ml & 0xffu) * nb);
       unsigned code = careful_code(v, c.e2lo, c.e2hi, nb, g.ka, g.kb);
       if (code < static_cast<unsigned>(nb)) {
-        const float s = ej.w + el.w, t = v - s;
-        const float H = fmaf(-t, t, 4.0f * ej.w * el.w);
-        const float S = s + v;
-        if (!(H > S * fmaf(g.ha, S, g.hb))) code = kCodeExact;
+        if (!heron_clean(v, __fmul_rn(ej.w, ej.w), 2.0f * ej.w, el.w, g.hm)) code = kCodeExact;
       }
       if (code == kCodeExact) {
         ++c.n_exact_tri;
@@ -567,7 +567,7 @@ __device__ __forceinline__ void enqueue_row(Cold& c, const Geom& g, int j, float
                                             int lb, int rhi, unsigned tab_adj, unsigned tab_last,
                                             unsigned nb_cs) {
   constexpr bool DIAG = MODE == 2;
-  const float a4 = 4.0f * ej.w;
+  const float aj = __fmul_rn(ej.w, ej.w), a2r = 2.0f * ej.w;
   ++c.n_flag_rows;
 #pragma unroll
   for (int r = 0; r < kReg; ++r) {
@@ -575,21 +575,16 @@ __device__ __forceinline__ void enqueue_row(Cold& c, const Geom& g, int j, float
     bool want = false;
     if (MODE == 0 || r < rhi) {
       if (!WEIGHTED && !HG) {
-        want = cand_flag(ej.x, ej.y, ej.z, ej.w, a4, el[r].x, el[r].y, el[r].z, el[r].w,
-                         DIAG ? static_cast<unsigned>(j > lr) : 1u, g.tab_scale, tab_adj, tab_last, nb_cs, g.ha,
-                         g.hb) != 0;
+        want = cand_flag(ej.x, ej.y, ej.z, aj, a2r, el[r].x, el[r].y, el[r].z, el[r].w,
+                         DIAG ? static_cast<unsigned>(j > lr) : 1u, g.tab_scale, tab_adj, tab_last, nb_cs,
+                         g.hm) != 0;
       } else {
         const float dx = ej.x - el[r].x;
         const float dy = ej.y - el[r].y;
         const float dz = ej.z - el[r].z;
         const float v = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
         const unsigned code = table_code(v, c.tab, g.tab_scale, g.tab_n);
-        const float b = el[r].w;
-        const float s = ej.w + b;
-        const float t = v - s;
-        const float H = fmaf(-t, t, a4 * b);
-        const float S = s + v;
-        const bool clean = H > S * fmaf(g.ha, S, g.hb);
+        const bool clean = heron_clean(v, aj, a2r, el[r].w, g.hm);
         want = code == kCodeCareful || (code < nb_cs && !clean);
         if (DIAG) want = want && (j > lr);
       }
@@ -743,7 +738,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
   const unsigned tab_last = tab_sh + static_cast<unsigned>(g.tab_n - 1);
   const unsigned hist_sh = static_cast<unsigned>(__cvta_generic_to_shared(hist_s)) + copy_off;
   const unsigned dummy = static_cast<unsigned>(__cvta_generic_to_shared(smem + L.scratch)) + 8u * lane;
-  const float tscale = g.tab_scale, ha = g.ha, hb = g.hb;
+  const float tscale = g.tab_scale, hm = g.hm;
 
   for (;;) {
     __syncthreads();
@@ -874,7 +869,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
             }
             if (code < static_cast<unsigned>(nb)) {
               acc = true;
-              ent = make_float4(dx, dy, dz, v);
+              ent = make_float4(dx, dy, dz, __fsqrt_rn(v));
               meta = code | (static_cast<unsigned>(s) << 8);
               pidx = j;
               w = q.w;
@@ -997,19 +992,19 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
           const int lr0 = lb + lane, lr1 = lr0 + 32, lr2 = lr0 + 64, lr3 = lr0 + 96;
           const float wsc = a.wscale;
           auto row = [&](float4 e, unsigned k, int jj, float wr) -> unsigned {
-            const float a4 = 4.0f * e.w;
+            const float aj = __fmul_rn(e.w, e.w), a2r = 2.0f * e.w;
             unsigned q = 0;
-            q |= cand_body<WEIGHTED, DIAG>(e.x, e.y, e.z, e.w, a4, L0.x, L0.y, L0.z, L0.w, k, K0, jj > lr0,
-                                           tscale, tab_adj, tab_last, nb_cs, ha, hb, dummy, wr, W0);
+            q |= cand_body<WEIGHTED, DIAG>(e.x, e.y, e.z, aj, a2r, L0.x, L0.y, L0.z, L0.w, k, K0, jj > lr0,
+                                           tscale, tab_adj, tab_last, nb_cs, hm, dummy, wr, W0);
             if (MODE == 0 || rhi > 1)
-              q |= cand_body<WEIGHTED, DIAG>(e.x, e.y, e.z, e.w, a4, L1.x, L1.y, L1.z, L1.w, k, K1, jj > lr1,
-                                             tscale, tab_adj, tab_last, nb_cs, ha, hb, dummy, wr, W1);
+              q |= cand_body<WEIGHTED, DIAG>(e.x, e.y, e.z, aj, a2r, L1.x, L1.y, L1.z, L1.w, k, K1, jj > lr1,
+                                             tscale, tab_adj, tab_last, nb_cs, hm, dummy, wr, W1);
             if (MODE == 0 || rhi > 2)
-              q |= cand_body<WEIGHTED, DIAG>(e.x, e.y, e.z, e.w, a4, L2.x, L2.y, L2.z, L2.w, k, K2, jj > lr2,
-                                             tscale, tab_adj, tab_last, nb_cs, ha, hb, dummy, wr, W2);
+              q |= cand_body<WEIGHTED, DIAG>(e.x, e.y, e.z, aj, a2r, L2.x, L2.y, L2.z, L2.w, k, K2, jj > lr2,
+                                             tscale, tab_adj, tab_last, nb_cs, hm, dummy, wr, W2);
             if (MODE == 0 || rhi > 3)
-              q |= cand_body<WEIGHTED, DIAG>(e.x, e.y, e.z, e.w, a4, L3.x, L3.y, L3.z, L3.w, k, K3, jj > lr3,
-                                             tscale, tab_adj, tab_last, nb_cs, ha, hb, dummy, wr, W3);
+              q |= cand_body<WEIGHTED, DIAG>(e.x, e.y, e.z, aj, a2r, L3.x, L3.y, L3.z, L3.w, k, K3, jj > lr3,
+                                             tscale, tab_adj, tab_last, nb_cs, hm, dummy, wr, W3);
             return __any_sync(FULL, q != 0) ? 1u : 0u;
           };
           int j = jb;
@@ -1052,7 +1047,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
             const unsigned o = static_cast<unsigned>(j - jb);
             const float4 ej = ej_base[o];
             const unsigned kj = (mj_base[o] & 0xffu) * kj_mul + (HG ? 0u : hist_sh);
-            const float a4 = 4.0f * ej.w;
+            const float aj = __fmul_rn(ej.w, ej.w), a2r = 2.0f * ej.w;
             const float wja = WEIGHTED ? wa * wj_base[o] * a.wscale : 0.0f;
             bool q = false;
 #pragma unroll
@@ -1063,12 +1058,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
               const float dz = ej.z - el[r].z;
               const float v = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
               const unsigned code = table_code(v, tab, g.tab_scale, g.tab_n);
-              const float b = el[r].w;
-              const float s = ej.w + b;
-              const float t = v - s;
-              const float H = fmaf(-t, t, a4 * b);
-              const float S = s + v;
-              const bool clean = H > S * fmaf(ha, S, hb);
+              const bool clean = heron_clean(v, aj, a2r, el[r].w, hm);
               bool ok = code < nb_cs;
               bool careful = code == kCodeCareful;
               if (DIAG) {

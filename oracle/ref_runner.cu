@@ -351,13 +351,16 @@ int ref_runner_count_rppi(const double* box, const double* edges, int n_edges, i
     }
     return 0;
   };
-  std::vector<std::vector<D4>> c2, c3;
-  if (grid(p2, n2, c2) || grid(p3, n3, c3)) {
+  // All three catalogues are gridded and uploaded per cell, as the
+  // reference does (source/cudaNcorr.cu:273-295), although its kernels read
+  // p1 from the flat copy.
+  std::vector<std::vector<D4>> c1, c2, c3;
+  if (grid(p1, n1, c1) || grid(p2, n2, c2) || grid(p3, n3, c3)) {
     g_ref.err = "point outside the reference's cell grid";
     return -2;
   }
-  std::vector<void*> h2(ncell, nullptr), h3(ncell, nullptr);
-  std::vector<int> s2(ncell), s3(ncell);
+  std::vector<void*> h1(ncell, nullptr), h2(ncell, nullptr), h3(ncell, nullptr);
+  std::vector<int> s1(ncell), s2(ncell), s3(ncell);
   auto put = [&](std::vector<std::vector<D4>>& cells, std::vector<void*>& h, std::vector<int>* sz) -> int {
     for (long i = 0; i < ncell; ++i) {
       (*sz)[i] = static_cast<int>(cells[i].size());
@@ -366,7 +369,7 @@ int ref_runner_count_rppi(const double* box, const double* edges, int n_edges, i
     }
     return 0;
   };
-  int rc = put(c2, h2, &s2) || put(c3, h3, &s3);
+  int rc = put(c1, h1, &s1) || put(c2, h2, &s2) || put(c3, h3, &s3);
   void *d_p1 = nullptr, *d_p2c = nullptr, *d_p3c = nullptr, *d_s2 = nullptr, *d_s3 = nullptr;
   void *d_sb = nullptr, *d_tc = nullptr;
   float kms = 0.0f;
@@ -412,6 +415,7 @@ int ref_runner_count_rppi(const double* box, const double* edges, int n_edges, i
     if (overflow) *overflow = ov;
   }
   for (long i = 0; i < ncell; ++i) {
+    cudaFree(h1[i]);
     cudaFree(h2[i]);
     cudaFree(h3[i]);
   }
