@@ -189,12 +189,19 @@ inline float f32_up(double x) {
 
 // FP32 error model (u = 2^-24).
 //  * List entries hold d = fl32(D), D the exact anchor-relative offset
-//    (computed in FP64), |D| < r_max. The pair estimate a = fl32(|d|^2)
-//    satisfies |a - A| <= 5u A; the triangle estimate v = fl32(|d_j - d_l|^2)
-//    satisfies |v - V| <= 7u V + 2u r_max^2 (componentwise error
-//    u(|D_j| + |D_l| + |X|), Cauchy-Schwarz, AM-GM on the cross term, three
-//    roundings in the sum of squares). ka, kb bound both with margin, also
-//    covering the rounding of the band arithmetic itself.
+//    (computed in FP64), |D| < r_max, and rho = sqrt_rn(a) of the pair
+//    estimate a = fl32(|d|^2), which satisfies |a - A| <= 5.1u A.
+//  * The pair loop forms the third side as v = p + s with p = -2 d_j.d_l
+//    (one product, two FMAs: error <= 6u r_max^2) and
+//    s = fma(rho_l, rho_l, fl(rho_j^2)) (within 13u r_max^2 of
+//    |d_j|^2 + |d_l|^2). |d_j - d_l|^2 itself is within 7u V + 2u r_max^2 of
+//    the reference's V (componentwise error u(|D_j| + |D_l|), Cauchy-Schwarz,
+//    AM-GM on the cross term). So |v - V| <= 8.1u V + 21u r_max^2. The
+//    exact-difference form used by the careful path and the pair stage is
+//    tighter. ka = 12u, kb = 32u r_max^2 bound all of them with margin, also
+//    covering the rounding of the band arithmetic itself. A slightly negative
+//    v (a side near zero) still maps to table entry 0, since
+//    kb * tab_scale < 0.25.
 //  * The prefilter estimate from cell-local coordinates (error <= 5u*cell +
 //    u|D| per component) satisfies |v - V| <= 14u V + 9u r_max^2; only used
 //    to skip candidates that are certainly out of range (pa, pb).
@@ -206,18 +213,20 @@ inline float f32_up(double x) {
 //    sqrtf(x2) > sqrtf(x3) errs by at most 6.5u r_max in p + q - r; so
 //    Q > 19.8u r_max^2 proves the triangle is kept. The list stores
 //    rho = sqrt_rn(a) with a within 5.1u A, so rho^2 is within 7.2u A and
-//    2 rho_j rho_l within 7.2u of 2 sqrt(AB). The kernel evaluates
-//    t = v - fma(rho_l, rho_l, rho_j^2) (error <= 30.7u r_max^2, with the
-//    7u V + 2u r_max^2 bound on v) and w = fma(2 rho_j, rho_l, -M) (error
-//    <= 16.5u r_max^2), and keeps the candidate when |t| < w: then
-//    Q > M - 47.2u r_max^2. M = 128u r_max^2 leaves a factor of two.
+//    2 rho_j rho_l within 7.2u of 2 sqrt(AB). The pair loop tests
+//    |p| < w with p = -2 d_j.d_l as above (C - A - B = -2 D_j.D_l exactly
+//    for the exact sides; |p - (C - A - B)| <= 10u r_max^2) and
+//    w = fma(2 rho_j, rho_l, -M) (error <= 16.5u r_max^2): then
+//    Q > M - 26.5u r_max^2. The careful path tests t = v - (a + b) with v
+//    from exact differences (error <= 30.7u r_max^2): Q > M - 47.2u r_max^2.
+//    M = 128u r_max^2 leaves a factor of two or more for both.
 // Margins are generous on purpose: a wider band only sends more candidates
 // to the exact FP64 path.
 inline void set_error_model(Geom& g) {
   const double u = std::ldexp(1.0, -24);
   const double r2 = g.sqr_rmax;
   g.ka = static_cast<float>(12.0 * u);
-  g.kb = static_cast<float>(4.0 * u * r2);
+  g.kb = static_cast<float>(32.0 * u * r2);
   g.hm = -f32_up(128.0 * u * r2);
   // Prefilter thresholds: candidates with v >= pre_hi or v <= pre_lo are
   // certainly outside (r_min^2, r_max^2).

@@ -22,9 +22,10 @@
 //           triangle. Work items are (l-tile of 128 entries, 32 j-entries);
 //           warps take items from a shared counter. A warp holds its l-tile in
 //           registers (4 per lane) and streams the j-entries as warp-wide
-//           broadcasts. Per candidate: |d_j - d_l|^2 in FP32, its bin from a
-//           shared-memory table, a margin test proving the reference's FP32
-//           triangle test, and one predicated shared atomic into the CTA's
+//           broadcasts. Per candidate: r3^2 in FP32 as
+//           rho_j^2 + rho_l^2 - 2 d_j.d_l, its bin from a shared-memory
+//           table, a margin test on d_j.d_l proving the reference's FP32
+//           triangle test, and one shared atomic into the CTA's
 //           (bin_j, bin_l, bin_3) histogram. Candidates whose FP32
 //           classification is not certain are queued per warp and settled by
 //           the exact FP64 restatement.
@@ -141,7 +142,10 @@ struct KArgs {
 __device__ __forceinline__ unsigned table_code(float v, const unsigned char* tab, float scale,
                                                int n) {
   const float y = fmaf(v, scale, 8388608.0f);
-  const int idx = min(__float_as_int(y) - 0x4B000000, n - 1);
+  // Unsigned, as in the PTX body: a slightly negative v (the estimate of a
+  // side near zero) rounds to index 0; anything below that or beyond the
+  // table wraps or clamps to the last entry.
+  const unsigned idx = min(static_cast<unsigned>(__float_as_int(y) - 0x4B000000), static_cast<unsigned>(n - 1));
   return tab[idx];
 }
 
@@ -221,67 +225,62 @@ __device__ __forceinline__ void red_shared_u64_if(unsigned addr, unsigned long l
       : "memory");
 }
 
-// One unweighted candidate (j, l) in hand-written PTX: the FP32 r3^2, its
-// table code, the Heron proof, the shared-memory histogram reduction, and the
-// flag "needs the careful/exact path". Every rounding is explicit (.rn),
-// matching the error model. kj/kl are byte offsets into the shared histogram
-// (kj includes its base address); `in` masks the candidate (diagonal tiles:
-// l < j). The reduction is unconditional: a candidate that does not count
-// adds to the lane's own scratch word `dummy` instead, which keeps the loop
-// free of the branch a predicated atomic compiles to.
-// Classification of one candidate, shared verbatim by the counting body and
-// the flag-only body so that both take bit-identical decisions.
+// Classification of one candidate (j, l) in hand-written PTX, shared verbatim
+// by the counting bodies and the flag-only body so that all take
+// bit-identical decisions. Operands: %1-%3 the row's offset d_j, %4 rho_j^2,
+// %5 2 rho_j, %6-%8 the column's offset scaled by -2, %9 rho_l, %12 `in`
+// (diagonal tiles: l < j), %13 table scale, %14/%15 table address bias and
+// last entry, %16 nb * code scale, %17 -M. With p = -2 d_j.d_l the third
+// side is v = p + (rho_l^2 + rho_j^2): three products and two adds instead of
+// three differences and three squares, and p itself is the quantity of the
+// margin test, |p| < 2 rho_j rho_l - M (|C - A - B| = |2 D_j.D_l| for the
+// exact sides). Every rounding is explicit (.rn), matching the error model.
+// Results: `upd` (the candidate counts in bin `code`) and, OR-ed into %0,
+// "needs the careful/exact path".
 #define NCORR_CAND_CLASSIFY                    \
-  "sub.rn.f32 dx, %1, %6;\n\t"                 \
-  "sub.rn.f32 dy, %2, %7;\n\t"                 \
-  "sub.rn.f32 dz, %3, %8;\n\t"                 \
-  "mul.rn.f32 v, dx, dx;\n\t"                  \
-  "fma.rn.f32 v, dy, dy, v;\n\t"               \
-  "fma.rn.f32 v, dz, dz, v;\n\t"               \
+  "mul.rn.f32 pp, %1, %6;\n\t"                 \
+  "fma.rn.f32 pp, %2, %7, pp;\n\t"             \
+  "fma.rn.f32 pp, %3, %8, pp;\n\t"             \
+  "fma.rn.f32 s, %9, %9, %4;\n\t"              \
+  "add.rn.f32 v, pp, s;\n\t"                   \
   "fma.rn.f32 y, v, %13, 0f4B000000;\n\t"      \
   "mov.b32 ia, y;\n\t"                         \
   "add.u32 ia, ia, %14;\n\t"                   \
   "min.u32 ia, ia, %15;\n\t"                   \
   "ld.shared.u8 code, [ia];\n\t"               \
-  "fma.rn.f32 s, %9, %9, %4;\n\t"              \
-  "sub.rn.f32 t, v, s;\n\t"                    \
-  "abs.f32 t, t;\n\t"                          \
+  "abs.f32 t, pp;\n\t"                         \
   "fma.rn.f32 H, %5, %9, %17;\n\t"             \
-  "setp.lt.f32 cl, t, H;\n\t"                  \
   "setp.lt.u32 ok, code, %16;\n\t"             \
-  "setp.eq.u32 car, code, 255;\n\t"            \
   NCORR_CAND_MASK                              \
-  "and.pred upd, ok, cl;\n\t"                  \
-  "not.pred ncl, cl;\n\t"                      \
-  "and.pred wq, ok, ncl;\n\t"                  \
-  "or.pred wq, wq, car;\n\t"                   \
-  "selp.u32 %0, 1, 0, wq;\n\t"
+  "setp.lt.and.f32 upd, t, H, ok;\n\t"         \
+  "setp.ge.and.f32 nco, t, H, ok;\n\t"         \
+  NCORR_CAND_WQ                                \
+  "@wq or.b32 %0, %0, 1;\n\t"
 
 // Diagonal tiles mask the candidate with `in` (operand 12).
 #define NCORR_CAND_MASK_ON           \
   "setp.ne.u32 inp, %12, 0;\n\t"     \
-  "and.pred ok, ok, inp;\n\t"        \
-  "and.pred car, car, inp;\n\t"
+  "and.pred ok, ok, inp;\n\t"
+#define NCORR_CAND_WQ_ON                      \
+  "setp.eq.and.u32 car, code, 255, inp;\n\t"  \
+  "or.pred wq, car, nco;\n\t"
+#define NCORR_CAND_WQ_OFF "setp.eq.or.u32 wq, code, 255, nco;\n\t"
 
-#define NCORR_CAND_DECLS                                         \
-  ".reg .f32 dx, dy, dz, v, y, s, t, H;\n\t"                   \
-  ".reg .b32 ia, code, key, adr;\n\t"                            \
-  ".reg .pred ok, cl, ncl, car, upd, wq, inp;\n\t"
+#define NCORR_CAND_DECLS                             \
+  ".reg .f32 pp, s, v, y, t, H;\n\t"                 \
+  ".reg .b32 ia, code, key, adr;\n\t"                \
+  ".reg .pred ok, upd, nco, car, wq, inp;\n\t"
 
-// One unweighted candidate (j, l) in hand-written PTX: the FP32 r3^2, its
-// table code, the Heron proof, the shared-memory histogram reduction, and the
-// flag "needs the careful/exact path". Every rounding is explicit (.rn),
-// matching the error model. kj/kl are byte offsets into the shared histogram
-// (kj includes its base address); `in` masks the candidate (diagonal tiles:
-// l < j). The reduction is unconditional: a candidate that does not count
-// adds to the lane's own scratch word `dummy` instead, which keeps the loop
-// free of the branch a predicated atomic compiles to.
+// One unweighted candidate: the classification, then the shared-memory
+// histogram reduction at byte offset kj + kl + code (kj includes the
+// histogram's base address). The reduction is unconditional: a candidate
+// that does not count adds to the lane's own scratch word `dummy` instead,
+// which keeps the loop free of the branch a predicated atomic compiles to.
 template <bool DIAG>
-__device__ __forceinline__ unsigned cand_count(float ex, float ey, float ez, float a, float a2r, float lx,
-                                               float ly, float lz, float b, unsigned kj, unsigned kl,
-                                               unsigned in, float tscale, unsigned tab_adj,
-                                               unsigned tab_last, unsigned nb_cs, float hm, unsigned dummy) {
-  unsigned q;
+__device__ __forceinline__ void cand_count(float ex, float ey, float ez, float a, float a2r, float lx, float ly,
+                                           float lz, float b, unsigned kj, unsigned kl, unsigned in, float tscale,
+                                           unsigned tab_adj, unsigned tab_last, unsigned nb_cs, float hm,
+                                           unsigned dummy, unsigned& q) {
 #define NCORR_CAND_COUNT_ASM                                                                          \
   asm volatile(                                                                                      \
       "{\n\t" NCORR_CAND_DECLS NCORR_CAND_CLASSIFY                                                     \
@@ -290,20 +289,24 @@ __device__ __forceinline__ unsigned cand_count(float ex, float ey, float ez, flo
       "selp.b32 adr, key, %18, upd;\n\t"                                                             \
       "red.shared.add.u32 [adr], 1;\n\t"                                                             \
       "}"                                                                                            \
-      : "=r"(q)                                                                                      \
+      : "+r"(q)                                                                                      \
       : "f"(ex), "f"(ey), "f"(ez), "f"(a), "f"(a2r), "f"(lx), "f"(ly), "f"(lz), "f"(b), "r"(kj), "r"(kl), \
-        "r"(in), "f"(tscale), "r"(tab_adj), "r"(tab_last), "r"(nb_cs), "f"(hm), "r"(dummy))
+        "r"(in), "f"(tscale), "r"(tab_adj), "r"(tab_last), "r"(nb_cs), "f"(hm), "r"(dummy)               \
+      : "memory")
   if (DIAG) {
 #define NCORR_CAND_MASK NCORR_CAND_MASK_ON
+#define NCORR_CAND_WQ NCORR_CAND_WQ_ON
     NCORR_CAND_COUNT_ASM;
+#undef NCORR_CAND_WQ
 #undef NCORR_CAND_MASK
   } else {
 #define NCORR_CAND_MASK ""
+#define NCORR_CAND_WQ NCORR_CAND_WQ_OFF
     NCORR_CAND_COUNT_ASM;
+#undef NCORR_CAND_WQ
 #undef NCORR_CAND_MASK
   }
 #undef NCORR_CAND_COUNT_ASM
-  return q;
 }
 
 // The weighted twin of cand_count: the same classification, then the
@@ -317,11 +320,10 @@ __device__ __forceinline__ unsigned cand_count(float ex, float ey, float ez, flo
 // thread's carry comes from its own atomic on the low word, so the 64-bit
 // total is exact however the adds interleave.
 template <bool DIAG>
-__device__ __forceinline__ unsigned cand_wsum(float ex, float ey, float ez, float a, float a2r, float lx,
-                                              float ly, float lz, float b, unsigned kj, unsigned kl,
-                                              unsigned in, float tscale, unsigned tab_adj, unsigned tab_last,
-                                              unsigned nb_cs, float hm, unsigned dummy, float wrow, float wl) {
-  unsigned q;
+__device__ __forceinline__ void cand_wsum(float ex, float ey, float ez, float a, float a2r, float lx, float ly,
+                                          float lz, float b, unsigned kj, unsigned kl, unsigned in, float tscale,
+                                          unsigned tab_adj, unsigned tab_last, unsigned nb_cs, float hm,
+                                          unsigned dummy, float wrow, float wl, unsigned& q) {
 #define NCORR_CAND_WSUM_ASM                                                                           \
   asm volatile(                                                                                      \
       "{\n\t" NCORR_CAND_DECLS                                                                        \
@@ -339,33 +341,38 @@ __device__ __forceinline__ unsigned cand_wsum(float ex, float ey, float ez, floa
       "add.u32 adrh, adr, 4;\n\t"                                                                    \
       "red.shared.add.u32 [adrh], whi;\n\t"                                                          \
       "}"                                                                                            \
-      : "=r"(q)                                                                                      \
+      : "+r"(q)                                                                                      \
       : "f"(ex), "f"(ey), "f"(ez), "f"(a), "f"(a2r), "f"(lx), "f"(ly), "f"(lz), "f"(b), "r"(kj), "r"(kl), \
-        "r"(in), "f"(tscale), "r"(tab_adj), "r"(tab_last), "r"(nb_cs), "f"(hm), "r"(dummy),           \
-        "f"(wrow), "f"(wl))
+        "r"(in), "f"(tscale), "r"(tab_adj), "r"(tab_last), "r"(nb_cs), "f"(hm), "r"(dummy), "f"(wrow),  \
+        "f"(wl)                                                                                      \
+      : "memory")
   if (DIAG) {
 #define NCORR_CAND_MASK NCORR_CAND_MASK_ON
+#define NCORR_CAND_WQ NCORR_CAND_WQ_ON
     NCORR_CAND_WSUM_ASM;
+#undef NCORR_CAND_WQ
 #undef NCORR_CAND_MASK
   } else {
 #define NCORR_CAND_MASK ""
+#define NCORR_CAND_WQ NCORR_CAND_WQ_OFF
     NCORR_CAND_WSUM_ASM;
+#undef NCORR_CAND_WQ
 #undef NCORR_CAND_MASK
   }
 #undef NCORR_CAND_WSUM_ASM
-  return q;
 }
 
 // Counting body of the shared-histogram path: count or weighted sum.
 template <bool WEIGHTED, bool DIAG>
-__device__ __forceinline__ unsigned cand_body(float ex, float ey, float ez, float a, float a2r, float lx,
-                                              float ly, float lz, float b, unsigned kj, unsigned kl,
-                                              unsigned in, float tscale, unsigned tab_adj, unsigned tab_last,
-                                              unsigned nb_cs, float hm, unsigned dummy, float wrow, float wl) {
+__device__ __forceinline__ void cand_body(float ex, float ey, float ez, float a, float a2r, float lx, float ly,
+                                          float lz, float b, unsigned kj, unsigned kl, unsigned in, float tscale,
+                                          unsigned tab_adj, unsigned tab_last, unsigned nb_cs, float hm,
+                                          unsigned dummy, float wrow, float wl, unsigned& q) {
   if (WEIGHTED)
-    return cand_wsum<DIAG>(ex, ey, ez, a, a2r, lx, ly, lz, b, kj, kl, in, tscale, tab_adj, tab_last, nb_cs, hm,
-                           dummy, wrow, wl);
-  return cand_count<DIAG>(ex, ey, ez, a, a2r, lx, ly, lz, b, kj, kl, in, tscale, tab_adj, tab_last, nb_cs, hm, dummy);
+    cand_wsum<DIAG>(ex, ey, ez, a, a2r, lx, ly, lz, b, kj, kl, in, tscale, tab_adj, tab_last, nb_cs, hm, dummy, wrow,
+                    wl, q);
+  else
+    cand_count<DIAG>(ex, ey, ez, a, a2r, lx, ly, lz, b, kj, kl, in, tscale, tab_adj, tab_last, nb_cs, hm, dummy, q);
 }
 
 // The same classification without the histogram update: 1 when the
@@ -373,15 +380,32 @@ __device__ __forceinline__ unsigned cand_body(float ex, float ey, float ez, floa
 __device__ __forceinline__ unsigned cand_flag(float ex, float ey, float ez, float a, float a2r, float lx,
                                               float ly, float lz, float b, unsigned in, float tscale,
                                               unsigned tab_adj, unsigned tab_last, unsigned nb_cs, float hm) {
-  unsigned q;
+  unsigned q = 0;
 #define NCORR_CAND_MASK NCORR_CAND_MASK_ON
+#define NCORR_CAND_WQ NCORR_CAND_WQ_ON
   asm volatile(
       "{\n\t" NCORR_CAND_DECLS NCORR_CAND_CLASSIFY "}"
-      : "=r"(q)
+      : "+r"(q)
       : "f"(ex), "f"(ey), "f"(ez), "f"(a), "f"(a2r), "f"(lx), "f"(ly), "f"(lz), "f"(b), "r"(0u), "r"(0u),
         "r"(in), "f"(tscale), "r"(tab_adj), "r"(tab_last), "r"(nb_cs), "f"(hm));
+#undef NCORR_CAND_WQ
 #undef NCORR_CAND_MASK
   return q;
+}
+
+// The classification in C++ with the same operations, for the paths that do
+// not run the PTX bodies (global histogram, weighted row re-examination).
+// `l` is the column entry as the pair loop holds it: (-2 d_l, rho_l).
+__device__ __forceinline__ void cand_classify(float ex, float ey, float ez, float a, float a2r, float4 l,
+                                              const unsigned char* tab, float scale, int n, float hm,
+                                              unsigned* code, bool* clean) {
+  float pp = __fmul_rn(ex, l.x);
+  pp = __fmaf_rn(ey, l.y, pp);
+  pp = __fmaf_rn(ez, l.z, pp);
+  const float s = __fmaf_rn(l.w, l.w, a);
+  const float v = __fadd_rn(pp, s);
+  *code = table_code(v, tab, scale, n);
+  *clean = fabsf(pp) < __fmaf_rn(a2r, l.w, hm);
 }
 
 __device__ __forceinline__ float lds_f32(unsigned addr) {
@@ -579,12 +603,9 @@ __device__ __forceinline__ void enqueue_row(Cold& c, const Geom& g, int j, float
                          DIAG ? static_cast<unsigned>(j > lr) : 1u, g.tab_scale, tab_adj, tab_last, nb_cs,
                          g.hm) != 0;
       } else {
-        const float dx = ej.x - el[r].x;
-        const float dy = ej.y - el[r].y;
-        const float dz = ej.z - el[r].z;
-        const float v = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-        const unsigned code = table_code(v, c.tab, g.tab_scale, g.tab_n);
-        const bool clean = heron_clean(v, aj, a2r, el[r].w, g.hm);
+        unsigned code;
+        bool clean;
+        cand_classify(ej.x, ej.y, ej.z, aj, a2r, el[r], c.tab, g.tab_scale, g.tab_n, g.hm, &code, &clean);
         want = code == kCodeCareful || (code < nb_cs && !clean);
         if (DIAG) want = want && (j > lr);
       }
@@ -956,13 +977,16 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
 #pragma unroll
         for (int r = 0; r < kReg; ++r) {
           const int l = lb + r * 32 + lane;
+          // Columns are held as (-2 d_l, rho_l); the padding (0, rho = 1e18)
+          // gives v = 1e36 and is rejected by the table for every row.
           if (l < k3) {
-            el[r] = l_in_smem ? l3.e[l] : l3.se[l - a.ks];
+            const float4 e = l_in_smem ? l3.e[l] : l3.se[l - a.ks];
+            el[r] = make_float4(-2.0f * e.x, -2.0f * e.y, -2.0f * e.z, e.w);
             const unsigned ml = l_in_smem ? l3.m[l] : l3.sm[l - a.ks];
             kl[r] = (ml & 0xffu) * nb_cs;
             wl[r] = WEIGHTED ? (l_in_smem ? l3.w[l] : l3.sw[l - a.ks]) : 0.0f;
           } else {
-            el[r] = make_float4(1.0e18f, 1.0e18f, 1.0e18f, 0.0f);
+            el[r] = make_float4(0.0f, 0.0f, 0.0f, 1.0e18f);
             kl[r] = 0;
             wl[r] = 0.0f;
           }
@@ -994,17 +1018,17 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
           auto row = [&](float4 e, unsigned k, int jj, float wr) -> unsigned {
             const float aj = __fmul_rn(e.w, e.w), a2r = 2.0f * e.w;
             unsigned q = 0;
-            q |= cand_body<WEIGHTED, DIAG>(e.x, e.y, e.z, aj, a2r, L0.x, L0.y, L0.z, L0.w, k, K0, jj > lr0,
-                                           tscale, tab_adj, tab_last, nb_cs, hm, dummy, wr, W0);
+            cand_body<WEIGHTED, DIAG>(e.x, e.y, e.z, aj, a2r, L0.x, L0.y, L0.z, L0.w, k, K0, jj > lr0, tscale,
+                                      tab_adj, tab_last, nb_cs, hm, dummy, wr, W0, q);
             if (MODE == 0 || rhi > 1)
-              q |= cand_body<WEIGHTED, DIAG>(e.x, e.y, e.z, aj, a2r, L1.x, L1.y, L1.z, L1.w, k, K1, jj > lr1,
-                                             tscale, tab_adj, tab_last, nb_cs, hm, dummy, wr, W1);
+              cand_body<WEIGHTED, DIAG>(e.x, e.y, e.z, aj, a2r, L1.x, L1.y, L1.z, L1.w, k, K1, jj > lr1,
+                                        tscale, tab_adj, tab_last, nb_cs, hm, dummy, wr, W1, q);
             if (MODE == 0 || rhi > 2)
-              q |= cand_body<WEIGHTED, DIAG>(e.x, e.y, e.z, aj, a2r, L2.x, L2.y, L2.z, L2.w, k, K2, jj > lr2,
-                                             tscale, tab_adj, tab_last, nb_cs, hm, dummy, wr, W2);
+              cand_body<WEIGHTED, DIAG>(e.x, e.y, e.z, aj, a2r, L2.x, L2.y, L2.z, L2.w, k, K2, jj > lr2,
+                                        tscale, tab_adj, tab_last, nb_cs, hm, dummy, wr, W2, q);
             if (MODE == 0 || rhi > 3)
-              q |= cand_body<WEIGHTED, DIAG>(e.x, e.y, e.z, aj, a2r, L3.x, L3.y, L3.z, L3.w, k, K3, jj > lr3,
-                                             tscale, tab_adj, tab_last, nb_cs, hm, dummy, wr, W3);
+              cand_body<WEIGHTED, DIAG>(e.x, e.y, e.z, aj, a2r, L3.x, L3.y, L3.z, L3.w, k, K3, jj > lr3,
+                                        tscale, tab_adj, tab_last, nb_cs, hm, dummy, wr, W3, q);
             return __any_sync(FULL, q != 0) ? 1u : 0u;
           };
           int j = jb;
@@ -1053,12 +1077,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
 #pragma unroll
             for (int r = 0; r < kReg; ++r) {
               if (MODE != 0 && r >= rhi) continue;
-              const float dx = ej.x - el[r].x;
-              const float dy = ej.y - el[r].y;
-              const float dz = ej.z - el[r].z;
-              const float v = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-              const unsigned code = table_code(v, tab, g.tab_scale, g.tab_n);
-              const bool clean = heron_clean(v, aj, a2r, el[r].w, hm);
+              unsigned code;
+              bool clean;
+              cand_classify(ej.x, ej.y, ej.z, aj, a2r, el[r], tab, g.tab_scale, g.tab_n, hm, &code, &clean);
               bool ok = code < nb_cs;
               bool careful = code == kCodeCareful;
               if (DIAG) {
