@@ -393,6 +393,67 @@ __device__ __forceinline__ unsigned cand_flag(float ex, float ey, float ez, floa
   return q;
 }
 
+// Four candidates of one row against one lane's four columns, unweighted and
+// off the diagonal (full l-tiles, most of the work): the classification of
+// NCORR_CAND_CLASSIFY operation for operation for each, then the four
+// histogram reductions. One asm statement lets the four table loads issue
+// before the first reduction; as four statements, each table load would wait
+// behind the previous candidate's reduction, which may touch the same
+// shared-memory word as far as the compiler can tell.
+#define NCORR_ROW_CLS(C, LX, LY, LZ, B)                  \
+  "mul.rn.f32 pp" #C ", %1, " LX ";\n\t"                 \
+  "fma.rn.f32 pp" #C ", %2, " LY ", pp" #C ";\n\t"       \
+  "fma.rn.f32 pp" #C ", %3, " LZ ", pp" #C ";\n\t"       \
+  "fma.rn.f32 s" #C ", " B ", " B ", %4;\n\t"            \
+  "add.rn.f32 v" #C ", pp" #C ", s" #C ";\n\t"           \
+  "fma.rn.f32 y" #C ", v" #C ", %7, 0f4B000000;\n\t"     \
+  "mov.b32 ia" #C ", y" #C ";\n\t"                       \
+  "add.u32 ia" #C ", ia" #C ", %8;\n\t"                  \
+  "min.u32 ia" #C ", ia" #C ", %9;\n\t"                  \
+  "ld.shared.u8 code" #C ", [ia" #C "];\n\t"
+#define NCORR_ROW_UPD(C, B, KL)                                      \
+  "abs.f32 t" #C ", pp" #C ";\n\t"                                   \
+  "fma.rn.f32 H" #C ", %5, " B ", %11;\n\t"                          \
+  "setp.lt.u32 ok" #C ", code" #C ", %10;\n\t"                       \
+  "setp.lt.and.f32 upd" #C ", t" #C ", H" #C ", ok" #C ";\n\t"       \
+  "setp.ge.and.f32 nco" #C ", t" #C ", H" #C ", ok" #C ";\n\t"       \
+  "setp.eq.or.u32 wq" #C ", code" #C ", 255, nco" #C ";\n\t"         \
+  "@wq" #C " or.b32 %0, %0, 1;\n\t"                                  \
+  "add.u32 key" #C ", %6, " KL ";\n\t"                               \
+  "add.u32 key" #C ", key" #C ", code" #C ";\n\t"                    \
+  "selp.b32 adr" #C ", key" #C ", %12, upd" #C ";\n\t"
+#define NCORR_ROW_DECL(C)                                                     \
+  ".reg .f32 pp" #C ", s" #C ", v" #C ", y" #C ", t" #C ", H" #C ";\n\t"      \
+  ".reg .b32 ia" #C ", code" #C ", key" #C ", adr" #C ";\n\t"                 \
+  ".reg .pred ok" #C ", upd" #C ", nco" #C ", wq" #C ";\n\t"
+
+__device__ __forceinline__ void row4_count(float ex, float ey, float ez, float a, float a2r, unsigned kj,
+                                           float tscale, unsigned tab_adj, unsigned tab_last, unsigned nb_cs,
+                                           float hm, unsigned dummy, const float4& l0, unsigned k0, const float4& l1,
+                                           unsigned k1, const float4& l2, unsigned k2, const float4& l3, unsigned k3,
+                                           unsigned& q) {
+  asm volatile(
+      "{\n\t" NCORR_ROW_DECL(0) NCORR_ROW_DECL(1) NCORR_ROW_DECL(2) NCORR_ROW_DECL(3)
+      NCORR_ROW_CLS(0, "%13", "%14", "%15", "%16") NCORR_ROW_CLS(1, "%18", "%19", "%20", "%21")
+      NCORR_ROW_CLS(2, "%23", "%24", "%25", "%26") NCORR_ROW_CLS(3, "%28", "%29", "%30", "%31")
+      NCORR_ROW_UPD(0, "%16", "%17") NCORR_ROW_UPD(1, "%21", "%22") NCORR_ROW_UPD(2, "%26", "%27")
+      NCORR_ROW_UPD(3, "%31", "%32")
+      "red.shared.add.u32 [adr0], 1;\n\t"
+      "red.shared.add.u32 [adr1], 1;\n\t"
+      "red.shared.add.u32 [adr2], 1;\n\t"
+      "red.shared.add.u32 [adr3], 1;\n\t"
+      "}"
+      : "+r"(q)
+      : "f"(ex), "f"(ey), "f"(ez), "f"(a), "f"(a2r), "r"(kj), "f"(tscale), "r"(tab_adj), "r"(tab_last), "r"(nb_cs),
+        "f"(hm), "r"(dummy), "f"(l0.x), "f"(l0.y), "f"(l0.z), "f"(l0.w), "r"(k0), "f"(l1.x), "f"(l1.y), "f"(l1.z),
+        "f"(l1.w), "r"(k1), "f"(l2.x), "f"(l2.y), "f"(l2.z), "f"(l2.w), "r"(k2), "f"(l3.x), "f"(l3.y), "f"(l3.z),
+        "f"(l3.w), "r"(k3)
+      : "memory");
+}
+#undef NCORR_ROW_CLS
+#undef NCORR_ROW_UPD
+#undef NCORR_ROW_DECL
+
 // The classification in C++ with the same operations, for the paths that do
 // not run the PTX bodies (global histogram, weighted row re-examination).
 // `l` is the column entry as the pair loop holds it: (-2 d_l, rho_l).
@@ -1018,6 +1079,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
           auto row = [&](float4 e, unsigned k, int jj, float wr) -> unsigned {
             const float aj = __fmul_rn(e.w, e.w), a2r = 2.0f * e.w;
             unsigned q = 0;
+            if (MODE == 0 && !WEIGHTED) {
+              row4_count(e.x, e.y, e.z, aj, a2r, k, tscale, tab_adj, tab_last, nb_cs, hm, dummy, L0, K0, L1, K1, L2,
+                         K2, L3, K3, q);
+              return __any_sync(FULL, q != 0) ? 1u : 0u;
+            }
             cand_body<WEIGHTED, DIAG>(e.x, e.y, e.z, aj, a2r, L0.x, L0.y, L0.z, L0.w, k, K0, jj > lr0, tscale,
                                       tab_adj, tab_last, nb_cs, hm, dummy, wr, W0, q);
             if (MODE == 0 || rhi > 1)
