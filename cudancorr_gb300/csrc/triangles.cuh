@@ -396,7 +396,8 @@ __device__ __forceinline__ unsigned cand_flag(float ex, float ey, float ez, floa
 // Four candidates of one row against one lane's four columns, unweighted and
 // off the diagonal (full l-tiles, most of the work): the classification of
 // NCORR_CAND_CLASSIFY operation for operation for each, then the four
-// histogram reductions. One asm statement lets the four table loads issue
+// histogram reductions. A candidate that needs the careful/exact path ORs
+// `rbit` (the row's bit in the work item) into q. One asm statement lets the four table loads issue
 // before the first reduction; as four statements, each table load would wait
 // behind the previous candidate's reduction, which may touch the same
 // shared-memory word as far as the compiler can tell.
@@ -418,7 +419,7 @@ __device__ __forceinline__ unsigned cand_flag(float ex, float ey, float ez, floa
   "setp.lt.and.f32 upd" #C ", t" #C ", H" #C ", ok" #C ";\n\t"       \
   "setp.ge.and.f32 nco" #C ", t" #C ", H" #C ", ok" #C ";\n\t"       \
   "setp.eq.or.u32 wq" #C ", code" #C ", 255, nco" #C ";\n\t"         \
-  "@wq" #C " or.b32 %0, %0, 1;\n\t"                                  \
+  "@wq" #C " or.b32 %0, %0, %33;\n\t"                                \
   "add.u32 key" #C ", %6, " KL ";\n\t"                               \
   "add.u32 key" #C ", key" #C ", code" #C ";\n\t"                    \
   "selp.b32 adr" #C ", key" #C ", %12, upd" #C ";\n\t"
@@ -431,7 +432,7 @@ __device__ __forceinline__ void row4_count(float ex, float ey, float ez, float a
                                            float tscale, unsigned tab_adj, unsigned tab_last, unsigned nb_cs,
                                            float hm, unsigned dummy, const float4& l0, unsigned k0, const float4& l1,
                                            unsigned k1, const float4& l2, unsigned k2, const float4& l3, unsigned k3,
-                                           unsigned& q) {
+                                           unsigned rbit, unsigned& q) {
   asm volatile(
       "{\n\t" NCORR_ROW_DECL(0) NCORR_ROW_DECL(1) NCORR_ROW_DECL(2) NCORR_ROW_DECL(3)
       NCORR_ROW_CLS(0, "%13", "%14", "%15", "%16") NCORR_ROW_CLS(1, "%18", "%19", "%20", "%21")
@@ -447,7 +448,7 @@ __device__ __forceinline__ void row4_count(float ex, float ey, float ez, float a
       : "f"(ex), "f"(ey), "f"(ez), "f"(a), "f"(a2r), "r"(kj), "f"(tscale), "r"(tab_adj), "r"(tab_last), "r"(nb_cs),
         "f"(hm), "r"(dummy), "f"(l0.x), "f"(l0.y), "f"(l0.z), "f"(l0.w), "r"(k0), "f"(l1.x), "f"(l1.y), "f"(l1.z),
         "f"(l1.w), "r"(k1), "f"(l2.x), "f"(l2.y), "f"(l2.z), "f"(l2.w), "r"(k2), "f"(l3.x), "f"(l3.y), "f"(l3.z),
-        "f"(l3.w), "r"(k3)
+        "f"(l3.w), "r"(k3), "r"(rbit)
       : "memory");
 }
 #undef NCORR_ROW_CLS
@@ -1081,7 +1082,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
             unsigned q = 0;
             if (MODE == 0 && !WEIGHTED) {
               row4_count(e.x, e.y, e.z, aj, a2r, k, tscale, tab_adj, tab_last, nb_cs, hm, dummy, L0, K0, L1, K1, L2,
-                         K2, L3, K3, q);
+                         K2, L3, K3, 1u, q);
               return __any_sync(FULL, q != 0) ? 1u : 0u;
             }
             cand_body<WEIGHTED, DIAG>(e.x, e.y, e.z, aj, a2r, L0.x, L0.y, L0.z, L0.w, k, K0, jj > lr0, tscale,
@@ -1102,6 +1103,21 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
             const unsigned e_sh = static_cast<unsigned>(__cvta_generic_to_shared(l2.e + jb));
             const unsigned m_sh = static_cast<unsigned>(__cvta_generic_to_shared(l2.m + jb));
             const unsigned w_sh = WEIGHTED ? static_cast<unsigned>(__cvta_generic_to_shared(l2.w + jb)) : 0u;
+            if (MODE == 0 && !WEIGHTED) {
+              // Full tile, counts: each row ORs its bit into the lane's flag
+              // word, and one warp reduction per work item gives the rows to
+              // re-examine.
+              unsigned qbits = 0;
+#pragma unroll 2
+              for (; j < je; ++j) {
+                const unsigned o = static_cast<unsigned>(j - jb);
+                const float4 e0 = lds_f4(e_sh + 16u * o);
+                const unsigned k0 = (lds_u32(m_sh + 4u * o) & 0xffu) * kj_mul + hist_sh;
+                row4_count(e0.x, e0.y, e0.z, __fmul_rn(e0.w, e0.w), 2.0f * e0.w, k0, tscale, tab_adj, tab_last, nb_cs,
+                           hm, dummy, L0, K0, L1, K1, L2, K2, L3, K3, 1u << o, qbits);
+              }
+              rowmask |= __reduce_or_sync(FULL, qbits);
+            }
 #if NCORR_ROW_UNROLL == 2
             for (; j + 1 < je; j += 2) {
               const unsigned o = static_cast<unsigned>(j - jb);
