@@ -888,8 +888,17 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
           s_do[s][d] = 0.0f;
         }
       }
-      s_start2[s] = ok ? s_it.c2.start[cell] : 0;
-      s_pre2[s + 1] = ok ? s_it.c2.count[cell] : 0;
+      int st2 = ok ? s_it.c2.start[cell] : 0;
+      int n2 = ok ? s_it.c2.count[cell] : 0;
+      if (SYM && s_sym6) {
+        // Six-fold loop: only neighbours after the anchor in cell order,
+        // so the slot's range starts past the anchor's sorted index.
+        const int lo = max(st2, ai + 1);
+        n2 = max(0, st2 + n2 - lo);
+        st2 = lo;
+      }
+      s_start2[s] = st2;
+      s_pre2[s + 1] = n2;
       if (!SYM) {
         s_start3[s] = ok ? s_it.c3.start[cell] : 0;
         s_pre3[s + 1] = ok ? s_it.c3.count[cell] : 0;
@@ -913,18 +922,32 @@ __global__ void __launch_bounds__(kThreads, 2) k_triangles(KArgs a) {
     auto build = [&](const Catalog& cat, const int* pre, const int* st, ListView& lv, int* counter) {
       const int total = pre[27];
       const int rounded = (total + 31) & ~31;
-      int s = 0;
+      // Software pipeline: the next round's point is loaded before this
+      // round's is classified, so two loads are in flight per thread.
+      int sn = 0, jn = 0;
+      float4 qn = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      if (warp * 32 + lane < total) {
+        const int first = warp * 32 + lane;
+        while (first >= pre[sn + 1]) ++sn;
+        jn = st[sn] + (first - pre[sn]);
+        qn = cat.pq[jn];
+      }
       for (int base = warp * 32; base < rounded; base += kThreads) {
         const int item = base + lane;
+        const int s = sn, j = jn;
+        const float4 q = qn;
+        const int next = item + kThreads;
+        if (next < total) {
+          while (next >= pre[sn + 1]) ++sn;
+          jn = st[sn] + (next - pre[sn]);
+          qn = cat.pq[jn];
+        }
         bool acc = false;
         float4 ent;
         unsigned meta = 0;
         int pidx = 0;
         float w = 0.0f;
         if (item < total) {
-          while (item >= pre[s + 1]) ++s;
-          const int j = st[s] + (item - pre[s]);
-          const float4 q = cat.pq[j];
           // Cell-local FP32 prefilter: skip candidates certainly out of range.
           const float fx = (q.x - qa.x) + s_do[s][0];
           const float fy = (q.y - qa.y) + s_do[s][1];
