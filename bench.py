@@ -165,24 +165,29 @@ def dist_setup():
     return world, rank, local
 
 
-def barrier_max(value: float, world: int) -> float:
+def _reduce(value: float, world: int, op) -> float:
+    """All-reduce of one number over the ranks: on the GPU under NCCL, on the
+    host under gloo (the CPU tests)."""
     if world == 1:
         return value
     import torch
     import torch.distributed as dist
-    t = torch.tensor([value], device="cuda", dtype=torch.float64)
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], device=dev, dtype=torch.float64)
+    dist.all_reduce(t, op=op)
     return float(t.item())
+
+
+def barrier_max(value: float, world: int) -> float:
+    """Slowest rank's time: the whole job's clock."""
+    import torch.distributed as dist
+    return value if world == 1 else _reduce(value, world, dist.ReduceOp.MAX)
 
 
 def barrier_sum(value: float, world: int) -> float:
-    if world == 1:
-        return value
-    import torch
+    """Units (triangles) counted by all ranks together."""
     import torch.distributed as dist
-    t = torch.tensor([value], device="cuda", dtype=torch.float64)
-    dist.all_reduce(t, op=dist.ReduceOp.SUM)
-    return float(t.item())
+    return value if world == 1 else _reduce(value, world, dist.ReduceOp.SUM)
 
 
 def barrier(world: int):
@@ -190,7 +195,8 @@ def barrier(world: int):
     if world > 1:
         import torch.distributed as dist
         dist.barrier()
-    torch.cuda.synchronize()
+    if torch.cuda.is_available():
+        torch.cuda.synchronize()
 
 
 def training_catalogue(name: str, i: int):
