@@ -11,10 +11,12 @@
 // the kernel's p2 and p3 roles, so a list per distinct catalogue serves both.
 // Phase B takes the list pairs (one row per warp, lanes over the row). An
 // FP32 estimate from anchor-relative offsets drops pairs that are certainly
-// cut; the rest are evaluated in FP64 with the reference's operations and
-// contractions, sorted and binned as getTriangleIndexRppi does
-// (source/device.cu:203-255), and added to the global histogram with one
-// atomic. With p2 == p3 in a box, each unordered pair is visited once: its
+// cut. In a box, the FP32 classifier of rppi_fast.cuh then settles almost
+// every pair with rigorous error bands; the pairs it leaves uncertain, and
+// every survey pair, are evaluated in FP64 with the reference's operations
+// and contractions, sorted and binned as getTriangleIndexRppi does
+// (source/device.cu:203-255). Each counted triangle is added to the global
+// histogram with one atomic. With p2 == p3 in a box, each unordered pair is visited once: its
 // two orderings give the same index unless two sides tie in rp^2 (the
 // reference's swap order then decides which pi goes with which side), and
 // the tie case computes both.
@@ -141,7 +143,7 @@ constexpr int kRppiThreads = 256;
 __device__ __forceinline__ void rppi_gather(const RppiArgs& a, const double4_16a& p1, const double4_16a* pd,
                                             const int* start, const int* s_off, const int* s_cell,
                                             const double (*s_sh)[3], int total, int* s_n, double4_16a* pos,
-                                            double2* ab, float4* rel, int cap) {
+                                            double2* ab, float4* rel, unsigned* meta, const double* sb, int cap) {
   const RppiGeom& g = a.g;
   for (int t = threadIdx.x; t < total; t += blockDim.x) {
     int s = 0;
@@ -168,8 +170,14 @@ __device__ __forceinline__ void rppi_gather(const RppiArgs& a, const double4_16a
       if (k < cap) {
         pos[k] = q;
         ab[k] = make_double2(x, y);
+        // Box: the classifier's per-side inputs, sqrt_rn(fl32(rp^2)) and the
+        // exact rp and pi bins (floor(sqrtf(pi^2)) as the reference forms it).
+        const float rho = g.survey ? 0.0f : __fsqrt_rn(__double2float_rn(x));
         rel[k] = make_float4(__double2float_rn(__dsub_rn(q.x, p1.x)), __double2float_rn(__dsub_rn(q.y, p1.y)),
-                             __double2float_rn(__dsub_rn(q.z, p1.z)), 0.0f);
+                             __double2float_rn(__dsub_rn(q.z, p1.z)), rho);
+        if (!g.survey)
+          meta[k] = static_cast<unsigned>(exact_bin(x, sb, g.nb)) |
+                    (static_cast<unsigned>(floorf(__fsqrt_rn(__double2float_rn(y)))) << 16);
       } else {
         atomicOr(a.flags, kFlagListOverflow);
       }
@@ -183,8 +191,13 @@ __global__ void __launch_bounds__(kRppiThreads) k_rppi(const __grid_constant__ R
   __shared__ double s_sb[kMaxEdges];
   __shared__ int s_off2[28], s_off3[28], s_cell[27];
   __shared__ double s_sh[27][3];
+  __shared__ float s_e2lo[kMaxEdges], s_e2hi[kMaxEdges];
   __shared__ int s_anchor, s_n2, s_n3;
-  for (int i = threadIdx.x; i <= g.nb; i += blockDim.x) s_sb[i] = g.sqr_bins[i];
+  for (int i = threadIdx.x; i <= g.nb; i += blockDim.x) {
+    s_sb[i] = g.sqr_bins[i];
+    s_e2lo[i] = g.fe2lo[i];
+    s_e2hi[i] = g.fe2hi[i];
+  }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   double4_16a* pos2 = a.l_pos + static_cast<size_t>(blockIdx.x) * 2 * a.cap;
   double4_16a* pos3 = SYM ? pos2 : pos2 + a.cap;
@@ -192,7 +205,9 @@ __global__ void __launch_bounds__(kRppiThreads) k_rppi(const __grid_constant__ R
   double2* ab3 = SYM ? ab2 : ab2 + a.cap;
   float4* rel2 = a.l_rel + static_cast<size_t>(blockIdx.x) * 2 * a.cap;
   float4* rel3 = SYM ? rel2 : rel2 + a.cap;
-  unsigned long long n_exact = 0;
+  unsigned* meta2 = a.l_meta + static_cast<size_t>(blockIdx.x) * 2 * a.cap;
+  unsigned* meta3 = SYM ? meta2 : meta2 + a.cap;
+  unsigned long long n_exact = 0, n_fast = 0;
   for (;;) {
     __syncthreads();  // the previous anchor's lists are no longer read
     if (threadIdx.x == 0) {
@@ -243,9 +258,11 @@ __global__ void __launch_bounds__(kRppiThreads) k_rppi(const __grid_constant__ R
       }
     }
     __syncthreads();
-    rppi_gather(a, p1, a.pd2, a.start2, s_off2, s_cell, s_sh, s_off2[27], &s_n2, pos2, ab2, rel2, a.cap);
+    rppi_gather(a, p1, a.pd2, a.start2, s_off2, s_cell, s_sh, s_off2[27], &s_n2, pos2, ab2, rel2, meta2, s_sb,
+                a.cap);
     if (!SYM)
-      rppi_gather(a, p1, a.pd3, a.start3, s_off3, s_cell, s_sh, s_off3[27], &s_n3, pos3, ab3, rel3, a.cap);
+      rppi_gather(a, p1, a.pd3, a.start3, s_off3, s_cell, s_sh, s_off3[27], &s_n3, pos3, ab3, rel3, meta3, s_sb,
+                  a.cap);
     __syncthreads();
     const int n2 = min(s_n2, a.cap);
     const int n3 = SYM ? n2 : min(s_n3, a.cap);
@@ -263,6 +280,7 @@ __global__ void __launch_bounds__(kRppiThreads) k_rppi(const __grid_constant__ R
       const double4_16a pj = pos2[j];
       const double2 abj = ab2[j];
       const float4 rj = rel2[j];
+      const unsigned mj = SURVEY ? 0u : meta2[j];
       const int l0 = (SYM && !SURVEY) ? j + 1 : 0;
       for (int l = l0 + lane; l < n3; l += 32) {
         if (SYM && l == j) continue;
@@ -274,24 +292,40 @@ __global__ void __launch_bounds__(kRppiThreads) k_rppi(const __grid_constant__ R
           if (dzf * dzf > g.f_pi_hi) continue;
           const float rpf = fmaf(dxf, dxf, dyf * dyf);
           if (rpf > g.f_rp_hi || rpf < g.f_rp_lo) continue;
-          ++n_exact;
-          const double4_16a pl = pos3[l];
-          const double dz = __dsub_rn(pj.z, pl.z);
-          const double pi3 = __dmul_rn(dz, dz);
-          if (!(pi3 < g.sqr_pimax)) continue;
-          const double rp3 = rp_exact(__dsub_rn(pj.x, pl.x), __dsub_rn(pj.y, pl.y), g.rp_pattern);
-          if (!(rp3 < g.sqr_rpmax && rp3 > g.sqr_rpmin)) continue;
-          const double2 abl = ab3[l];
-          idx = rppi_index(abj.x, abl.x, rp3, abj.y, abl.y, pi3, s_sb, g.nb, g.npi);
-          if (idx < 0) continue;
-          if (WEIGHTED) w = __dmul_rn(__dmul_rn(p1.w, pj.w), pl.w);
-          if (SYM) {
-            // The (l, j) ordering: same sides, anchor sides swapped.
-            if (abj.x == abl.x || abj.x == rp3 || abl.x == rp3)
-              idx2 = rppi_index(abl.x, abj.x, rp3, abl.y, abj.y, pi3, s_sb, g.nb, g.npi);
-            else
-              idx2 = idx;
-            if (WEIGHTED) w2 = __dmul_rn(__dmul_rn(p1.w, pl.w), pj.w);
+          // FP32 classification; the FP64 restatement below settles what it
+          // leaves uncertain.
+          const long long fi = rppi_fast_index(rj.x, rj.y, rj.z, rj.w, mj, rl.x, rl.y, rl.z, rl.w, meta3[l], g.fast,
+                                               s_e2lo, s_e2hi);
+          if (fi == -1) continue;
+          if (fi >= 0) {
+            ++n_fast;
+            idx = fi;
+            idx2 = fi;  // no rp^2 ties when the classifier is certain
+            if (WEIGHTED) {
+              const double wl = pos3[l].w;
+              w = __dmul_rn(__dmul_rn(p1.w, pj.w), wl);
+              w2 = __dmul_rn(__dmul_rn(p1.w, wl), pj.w);
+            }
+          } else {
+            ++n_exact;
+            const double4_16a pl = pos3[l];
+            const double dz = __dsub_rn(pj.z, pl.z);
+            const double pi3 = __dmul_rn(dz, dz);
+            if (!(pi3 < g.sqr_pimax)) continue;
+            const double rp3 = rp_exact(__dsub_rn(pj.x, pl.x), __dsub_rn(pj.y, pl.y), g.rp_pattern);
+            if (!(rp3 < g.sqr_rpmax && rp3 > g.sqr_rpmin)) continue;
+            const double2 abl = ab3[l];
+            idx = rppi_index(abj.x, abl.x, rp3, abj.y, abl.y, pi3, s_sb, g.nb, g.npi);
+            if (idx < 0) continue;
+            if (WEIGHTED) w = __dmul_rn(__dmul_rn(p1.w, pj.w), pl.w);
+            if (SYM) {
+              // The (l, j) ordering: same sides, anchor sides swapped.
+              if (abj.x == abl.x || abj.x == rp3 || abl.x == rp3)
+                idx2 = rppi_index(abl.x, abj.x, rp3, abl.y, abj.y, pi3, s_sb, g.nb, g.npi);
+              else
+                idx2 = idx;
+              if (WEIGHTED) w2 = __dmul_rn(__dmul_rn(p1.w, pl.w), pj.w);
+            }
           }
         } else {
           if (fmaf(dzf, dzf, fmaf(dxf, dxf, dyf * dyf)) > g.f_s_hi) continue;
@@ -343,6 +377,7 @@ __global__ void __launch_bounds__(kRppiThreads) k_rppi(const __grid_constant__ R
     }
   }
   if (n_exact) atomicAdd(&a.stats[3], n_exact);
+  if (n_fast) atomicAdd(&a.stats[4], n_fast);
 }
 
 template <bool SURVEY, bool SYM, bool WEIGHTED>
@@ -438,6 +473,25 @@ int rppi_init(ncorr_handle* h, const double box[3], const double* edges, int n_e
   g.f_rp_lo = rpmin > 2.0 * slack ? f32_down((rpmin - 2.0 * slack) * (rpmin - 2.0 * slack)) : 0.0f;
   const double smax = std::sqrt(g.sqr_rmax);
   g.f_s_hi = f32_up((smax + 2.0 * slack) * (smax + 2.0 * slack));
+  // The box-mode FP32 classifier: its bands and margins, derived in
+  // rppi_fast.cuh (u = 2^-24).
+  const double u = std::ldexp(1.0, -24);
+  RppiFast& f = g.fast;
+  f.epi = f32_up(64.0 * u * g.sqr_pimax);
+  f.erp = f32_up(128.0 * u * g.sqr_rpmax);
+  f.pimax2 = static_cast<float>(g.sqr_pimax);  // nPi^2 <= 2^24: exact
+  f.rpmax2_lo = f32_down(g.sqr_rpmax);
+  f.rpmax2_hi = f32_up(g.sqr_rpmax);
+  f.rpmin2_lo = f32_down(g.sqr_rpmin);
+  f.rpmin2_hi = f32_up(g.sqr_rpmin);
+  f.hm = -f32_up(128.0 * u * g.sqr_rpmax);
+  f.pmarg = f32_up(16.0 * u * g.sqr_pimax);
+  f.nb = nb;
+  f.npi = num_minor_bins;
+  for (int i = 0; i < n_edges; ++i) {
+    g.fe2lo[i] = f32_down(g.sqr_bins[i]);
+    g.fe2hi[i] = f32_up(g.sqr_bins[i]);
+  }
   // Output tables (source/cudaNcorr.cu:195-213).
   for (int i = 0; i < nb; ++i)
     for (int j = i; j < nb; ++j)
@@ -562,6 +616,7 @@ int rppi_run(ncorr_handle* h, const double4_16a* d1, int n1, const double4_16a* 
   CU(h->rp_pos.ensure(slab_n * sizeof(double4_16a)));
   CU(h->rp_ab.ensure(slab_n * sizeof(double2)));
   CU(h->rp_rel.ensure(slab_n * sizeof(float4)));
+  CU(h->rp_meta.ensure(slab_n * sizeof(unsigned)));
   const size_t hist_n = static_cast<size_t>(g.nbins) + 1;
   CU(h->d_hist.ensure(hist_n * sizeof(double)));
   CU(cudaMemsetAsync(h->d_hist.p, 0, hist_n * sizeof(double), st));
@@ -580,6 +635,7 @@ int rppi_run(ncorr_handle* h, const double4_16a* d1, int n1, const double4_16a* 
   a.l_pos = h->rp_pos.as<double4_16a>();
   a.l_ab = h->rp_ab.as<double2>();
   a.l_rel = h->rp_rel.as<float4>();
+  a.l_meta = h->rp_meta.as<unsigned>();
   a.cap = cap;
   a.hist_u = weighted ? nullptr : h->d_hist.as<unsigned long long>();
   a.hist_w = weighted ? h->d_hist.as<double>() : nullptr;
@@ -628,6 +684,7 @@ int rppi_run(ncorr_handle* h, const double4_16a* d1, int n1, const double4_16a* 
   s.n_pair_evals = st_host[1];
   s.n_pairs = st_host[2];
   s.n_exact_tris = st_host[3];
+  s.n_queued = st_host[4];
   s.triangles = weighted ? 0 : total;
   s.weighted = weighted ? 1 : 0;
   s.symmetric = (sym && !g.survey) ? 2 : 1;

@@ -7,6 +7,7 @@
 // line of sight = the sum of the three position vectors).
 #pragma once
 #include "engine.cuh"
+#include "rppi_fast.cuh"
 
 namespace ncorr_gb300 {
 
@@ -31,6 +32,10 @@ struct RppiGeom {
   float f_rp_lo;     // box: rp^2 estimate < f_rp_lo  => rp^2 <= rpMin^2
   float f_s_hi;      // survey: s^2 estimate > f_s_hi => s^2 >= sqrRMax
   long long nbins;   // nb^3 * nPi^2
+  // Box mode: the FP32 classifier (rppi_fast.cuh) and its bin-edge bounds.
+  RppiFast fast;
+  float fe2lo[kMaxEdges];  // largest float <= edges^2
+  float fe2hi[kMaxEdges];  // smallest float >= edges^2
 };
 
 struct RppiArgs {
@@ -46,13 +51,15 @@ struct RppiArgs {
   // Per-CTA neighbour lists (two lists of `cap` entries per CTA).
   double4_16a* l_pos;  // neighbour (its image in a box), weight
   double2* l_ab;       // box: (rp^2, pi^2) to the anchor; survey: (sqrS, 0)
-  float4* l_rel;       // FP32 anchor-relative offset
+  float4* l_rel;       // FP32 anchor-relative offset; box: .w = sqrt_rn(fl32(rp^2))
+  unsigned* l_meta;    // box: exact rp bin | pi bin << 16 of the anchor side
   int cap;
   unsigned long long* hist_u;  // nbins + 1 counts; [nbins] collects indices past the end
   double* hist_w;              // nbins + 1 weighted sums (same layout)
   int* work;
   int* flags;
-  unsigned long long* stats;   // [0] anchors, [1] scanned, [2] candidate pairs, [3] exact evaluations
+  unsigned long long* stats;   // [0] anchors, [1] scanned, [2] candidate pairs, [3] FP64 evaluations,
+                               // [4] pairs settled by the FP32 classifier
 };
 
 }  // namespace ncorr_gb300

@@ -55,10 +55,11 @@ typedef struct ncorr_stats {
   uint64_t n_pair_evals;   /* candidate neighbours scanned (27-cell walk) */
   uint64_t n_pairs;        /* candidate triangles W (neighbour pairs visited) */
   uint64_t n_exact_pairs;  /* neighbours settled by the FP64 path */
-  uint64_t n_exact_tris;   /* triangles settled by the FP64 path */
+  uint64_t n_exact_tris;   /* triangles (rppi: pairs) settled by the FP64 path */
   uint64_t triangles;      /* sum of the full histogram (count mode) */
   uint64_t n_flagged_rows; /* neighbour rows re-examined for uncertain candidates */
-  uint64_t n_queued;       /* candidates settled by the careful band or the FP64 path */
+  uint64_t n_queued;       /* threeD: candidates settled by the careful band or the FP64 path;
+                              rppi: pairs settled by the box-mode FP32 classifier */
   int weighted;            /* 1: some weight != 1.0 (fixed-point weighted sums) */
   int symmetric;           /* orderings each visited triangle stands for: 1 (all (j,l)),
                               2 (p2 == p3: pairs j<l), 6 (p1 == p2 == p3 in a geometry

@@ -152,3 +152,25 @@ def test_rppi_golden_reference_outputs(oracle, meta_path):
     else:
         assert np.array_equal(h, ref)
         assert ov == meta["overflow"]
+
+
+def test_rppi_fp32_classifier_agrees_with_the_exact_computation(tmp_path):
+    """The box-mode FP32 classifier (cudancorr_gb300/csrc/rppi_fast.cuh),
+    compiled for the host, against an FP64 restatement of the reference on
+    random and adversarial triangles (third side on a bin edge or equal to an
+    anchor side, pi3 next to k^2, nearly collinear): whenever it answers, the
+    answer is the reference's."""
+    import shutil
+    import subprocess
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    src = GOLDEN.parent / "cpp" / "rppi_fast_check.cu"
+    exe = tmp_path / "rppi_fast_check"
+    r = subprocess.run([nvcc, "-std=c++17", "-O2", "-Xcompiler", "-ffp-contract=off", "-o", str(exe), str(src)],
+                       capture_output=True, text=True)
+    if r.returncode != 0:
+        pytest.skip(f"nvcc could not build the host check: {r.stderr[:200]}")
+    for seed in (1, 2):
+        out = subprocess.run([str(exe), "200000", str(seed)], capture_output=True, text=True)
+        assert out.returncode == 0, out.stdout + out.stderr
+        n = dict(zip(out.stdout.split()[0::2], map(int, out.stdout.split()[1::2])))
+        assert n["mismatches"] == 0 and n["certain"] > n["checked"] // 4 and n["counted"] > 0
