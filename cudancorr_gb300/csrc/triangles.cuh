@@ -598,7 +598,7 @@ __device__ __noinline__ void cold_flush_exact(Cold& c) {
 }
 
 // Settles the queued candidates, 32 per round: the explicit FP32 band and the
-// Heron test decide most; the rest go to the exact buffer.
+// margin test of the triangle decide most; the rest go to the exact buffer.
 template <bool SURVEY, bool WEIGHTED, bool HG>
 __device__ __noinline__ void cold_drain(Cold& c) {
   const KArgs& a = *c.a;
