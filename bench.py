@@ -148,6 +148,16 @@ def cpu_baseline(p, box, edges, budget_s: float = 12.0) -> dict:
                       f"{dt:.1f} s, oracle/ncorr_oracle.cpp neighbour-list form"}
 
 
+def engine_launches(n_distinct: int, sym: bool, learned: bool = False, rppi: bool = False) -> int:
+    """Kernels one calculateD1D2D3 launches: per distinct catalogue the cell
+    list (assign, scan, scatter), the neighbourhood bound per list catalogue,
+    then the triangle kernel with its exact pass and fold (threeD) or the
+    rppi kernel; the learned schedule adds the features, the prediction and
+    seven queue-building kernels."""
+    n = 3 * n_distinct + (1 if sym else 2) + (1 if rppi else 3)
+    return n + (9 if learned else 0)
+
+
 def dist_setup():
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -351,7 +361,7 @@ def run_engine(args) -> dict:
                      "W": int(st_last["n_pairs"]), "P": int(st_last["n_pair_evals"]),
                      "peak_basis": "152 SMs x 128 FP32 lanes x 2 x median sampled SM clock "
                                    "(MEASURED_PEAKS.json has no FP32 entry)"},
-        "gpu_launches": 6 * args.steps,
+        "gpu_launches": engine_launches(1 if p1 is p else 2, True, args.schedule == "learned") * args.steps,
         "clocks": clocks,
         "exact_path": {"pairs": int(st_last["n_exact_pairs"]), "triangles": int(st_last["n_exact_tris"]),
                        "flagged_rows": int(st_last["n_flagged_rows"]), "queued": int(st_last["n_queued"])},
@@ -616,7 +626,8 @@ def run_survey(args) -> dict:
                      "kernel_ms": sum(kernel_ms) / args.steps,
                      "work": "8 flops x (candidate triangles W + pair-stage evaluations P), four calls",
                      "peak_basis": "152 SMs x 128 FP32 lanes x 2 x median sampled SM clock"},
-        "gpu_launches": 6 * len(runs) * args.steps,
+        "gpu_launches": sum(engine_launches(2 if c[1] == c[2] else 3, c[1] == c[2]) for c, _, _, _ in runs)
+        * args.steps,
         "clocks": clocks,
         "per_triple_ms": {c: statistics.mean(v) for c, v in per.items()},
         "precision_vs_fp64_oracle": precision,
@@ -720,7 +731,7 @@ def run_rppi(args) -> dict:
                      "pairs_visited": int(st_last["n_pairs"]), "pairs_fp32_classifier": int(st_last["n_queued"]),
                      "pairs_fp64": int(st_last["n_exact_tris"]),
                      "peak_basis": "152 SMs x 128 FP32 lanes x 2 x median sampled SM clock"},
-        "gpu_launches": 4 * args.steps,
+        "gpu_launches": engine_launches(1, True, rppi=True) * args.steps,
         "clocks": clocks,
         "n_out": n_out,
     }
