@@ -1,6 +1,8 @@
 // C ABI of the engine (include/ncorr_gb300.h): handle life cycle, host
 // orchestration of one calculateD1D2D3, result compaction.
 #include <mutex>
+#include <new>
+#include <stdexcept>
 
 #include "host.cuh"
 
@@ -421,7 +423,12 @@ int ncorr_create_rppi(const double box[3], int bin_type, const double* edges, in
   for (int i = 1; i < n_edges; ++i) h->mids.push_back((edges[i] + edges[i - 1]) / 2.0);
   std::memset(&h->g, 0, sizeof(h->g));
   std::memset(&h->stats, 0, sizeof(h->stats));
-  int rc = rppi_init(h, box, edges, n_edges, num_minor_bins, is_survey, ori);
+  int rc;
+  try {
+    rc = rppi_init(h, box, edges, n_edges, num_minor_bins, is_survey, ori);
+  } catch (const std::bad_alloc&) {
+    rc = fail(NCORR_ERR_CAPACITY, "host memory exhausted (output tables of nb^3 * numMinorBins^2 entries)");
+  }
   if (rc) {
     delete h;
     return rc;
@@ -461,8 +468,8 @@ void ncorr_destroy(ncorr_handle* h) {
   delete h;
 }
 
-int ncorr_calculate_d1d2d3(ncorr_handle* h, const double* p1, int64_t n1, const double* p2,
-                           int64_t n2, const double* p3, int64_t n3) {
+static int calculate_host(ncorr_handle* h, const double* p1, int64_t n1, const double* p2, int64_t n2,
+                          const double* p3, int64_t n3) {
   if (!h) return fail(NCORR_ERR_INVALID_ARGUMENT, "null handle");
   int rc;
   if ((rc = validate_catalog_ptr(p1, n1)) || (rc = validate_catalog_ptr(p2, n2)) ||
@@ -494,9 +501,8 @@ int ncorr_calculate_d1d2d3(ncorr_handle* h, const double* p1, int64_t n1, const 
              static_cast<int>(n3), st, p1, p2, p3);
 }
 
-int ncorr_calculate_d1d2d3_device(ncorr_handle* h, const double* d_p1, int64_t n1,
-                                  const double* d_p2, int64_t n2, const double* d_p3, int64_t n3,
-                                  void* stream) {
+static int calculate_device(ncorr_handle* h, const double* d_p1, int64_t n1, const double* d_p2, int64_t n2,
+                            const double* d_p3, int64_t n3, void* stream) {
   if (!h) return fail(NCORR_ERR_INVALID_ARGUMENT, "null handle");
   int rc;
   if ((rc = validate_catalog_ptr(d_p1, n1)) || (rc = validate_catalog_ptr(d_p2, n2)) ||
@@ -513,6 +519,31 @@ int ncorr_calculate_d1d2d3_device(ncorr_handle* h, const double* d_p1, int64_t n
   return run(h, reinterpret_cast<const double4_16a*>(d_p1), static_cast<int>(n1),
              reinterpret_cast<const double4_16a*>(d_p2), static_cast<int>(n2),
              reinterpret_cast<const double4_16a*>(d_p3), static_cast<int>(n3), st, d_p1, d_p2, d_p3);
+}
+
+// Host allocations (result tables, read-back buffers) may throw; nothing
+// throws across the C ABI.
+int ncorr_calculate_d1d2d3(ncorr_handle* h, const double* p1, int64_t n1, const double* p2,
+                           int64_t n2, const double* p3, int64_t n3) {
+  try {
+    return calculate_host(h, p1, n1, p2, n2, p3, n3);
+  } catch (const std::bad_alloc&) {
+    return fail(NCORR_ERR_CAPACITY, "host memory exhausted");
+  } catch (const std::exception& e) {
+    return fail(NCORR_ERR_INVALID_ARGUMENT, e.what());
+  }
+}
+
+int ncorr_calculate_d1d2d3_device(ncorr_handle* h, const double* d_p1, int64_t n1,
+                                  const double* d_p2, int64_t n2, const double* d_p3, int64_t n3,
+                                  void* stream) {
+  try {
+    return calculate_device(h, d_p1, n1, d_p2, n2, d_p3, n3, stream);
+  } catch (const std::bad_alloc&) {
+    return fail(NCORR_ERR_CAPACITY, "host memory exhausted");
+  } catch (const std::exception& e) {
+    return fail(NCORR_ERR_INVALID_ARGUMENT, e.what());
+  }
 }
 
 int64_t ncorr_num_out(const ncorr_handle* h) {

@@ -1,12 +1,16 @@
-// Catalogue input and result output of the C ABI: the counterparts of the
+// Catalogue input and result output of the C ABI (each entry point catches
+// what the host code may throw, so nothing crosses the ABI): the counterparts of the
 // reference's text reader, result writers and random catalogue
 // (include/utils.hpp, source/utils.cu:29-52, :119-208 of cudaNcorr). Host
 // code only; the engine's kernels never read files.
 #include <cstdio>
+#include <new>
+#include <stdexcept>
 #include <fstream>
 #include <random>
 #include <sstream>
 #include <string>
+#include <system_error>
 #include <thread>
 
 #include "host.cuh"
@@ -48,7 +52,7 @@ int write_rows(const char* filename, const double* const* cols, int ncols, int64
 
 extern "C" {
 
-int ncorr_write_three_d(const char* filename, const double* tri_bins, const double* counts, int64_t n) {
+static int write_three_d_impl(const char* filename, const double* tri_bins, const double* counts, int64_t n) {
   if (n > 0 && (!tri_bins || !counts)) return fail(NCORR_ERR_INVALID_ARGUMENT, "null array");
   std::vector<double> r1(static_cast<size_t>(std::max<int64_t>(n, 0))), r2(r1.size()), r3(r1.size());
   for (int64_t i = 0; i < n; ++i) {
@@ -60,7 +64,7 @@ int ncorr_write_three_d(const char* filename, const double* tri_bins, const doub
   return write_rows(filename, cols, 4, n);
 }
 
-int ncorr_write_rppi(const char* filename, const double* tri_bins, const double* pi_bins, const double* counts,
+static int write_rppi_impl(const char* filename, const double* tri_bins, const double* pi_bins, const double* counts,
                      int64_t n) {
   if (n > 0 && (!tri_bins || !pi_bins || !counts)) return fail(NCORR_ERR_INVALID_ARGUMENT, "null array");
   const size_t m = static_cast<size_t>(std::max<int64_t>(n, 0));
@@ -76,7 +80,7 @@ int ncorr_write_rppi(const char* filename, const double* tri_bins, const double*
   return write_rows(filename, cols, 6, n);
 }
 
-int ncorr_read_catalog_txt(const char* filename, const double box[3], const int pos_columns[4], double* out,
+static int read_catalog_txt_impl(const char* filename, const double box[3], const int pos_columns[4], double* out,
                            int64_t cap, int64_t* n) {
   if (!filename || !box || !pos_columns || !n) return fail(NCORR_ERR_INVALID_ARGUMENT, "null argument");
   *n = 0;
@@ -118,7 +122,7 @@ int ncorr_read_catalog_txt(const char* filename, const double box[3], const int 
   return NCORR_OK;
 }
 
-int ncorr_random_catalog(int64_t n, const double box[3], uint64_t seed, double* out) {
+static int random_catalog_impl(int64_t n, const double box[3], uint64_t seed, double* out) {
   if (n < 0 || !box || (n > 0 && !out)) return fail(NCORR_ERR_INVALID_ARGUMENT, "bad argument");
   for (int d = 0; d < 3; ++d)
     if (!(box[d] > 0.0) || !std::isfinite(box[d])) return fail(NCORR_ERR_INVALID_ARGUMENT, "box sides must be positive");
@@ -145,10 +149,61 @@ int ncorr_random_catalog(int64_t n, const double box[3], uint64_t seed, double* 
     }
   };
   std::vector<std::thread> pool;
-  for (unsigned t = 1; t < nth; ++t) pool.emplace_back(work, t);
+  unsigned started = 1;  // stripes handed to threads (stripe 0 runs here)
+  try {
+    for (unsigned t = 1; t < nth; ++t) {
+      pool.emplace_back(work, t);
+      ++started;
+    }
+  } catch (const std::system_error&) {
+    // Fewer threads than asked for: the remaining stripes run below.
+  }
+  for (unsigned t = started; t < nth; ++t) work(t);
   work(0);
   for (auto& th : pool) th.join();
   return NCORR_OK;
+}
+
+int ncorr_write_three_d(const char* filename, const double* tri_bins, const double* counts, int64_t n) {
+  try {
+    return write_three_d_impl(filename, tri_bins, counts, n);
+  } catch (const std::bad_alloc&) {
+    return fail(NCORR_ERR_CAPACITY, "host memory exhausted");
+  } catch (const std::exception& e) {
+    return fail(NCORR_ERR_INVALID_ARGUMENT, e.what());
+  }
+}
+
+int ncorr_write_rppi(const char* filename, const double* tri_bins, const double* pi_bins, const double* counts,
+                     int64_t n) {
+  try {
+    return write_rppi_impl(filename, tri_bins, pi_bins, counts, n);
+  } catch (const std::bad_alloc&) {
+    return fail(NCORR_ERR_CAPACITY, "host memory exhausted");
+  } catch (const std::exception& e) {
+    return fail(NCORR_ERR_INVALID_ARGUMENT, e.what());
+  }
+}
+
+int ncorr_read_catalog_txt(const char* filename, const double box[3], const int pos_columns[4], double* out,
+                           int64_t cap, int64_t* n) {
+  try {
+    return read_catalog_txt_impl(filename, box, pos_columns, out, cap, n);
+  } catch (const std::bad_alloc&) {
+    return fail(NCORR_ERR_CAPACITY, "host memory exhausted");
+  } catch (const std::exception& e) {
+    return fail(NCORR_ERR_INVALID_ARGUMENT, e.what());
+  }
+}
+
+int ncorr_random_catalog(int64_t n, const double box[3], uint64_t seed, double* out) {
+  try {
+    return random_catalog_impl(n, box, seed, out);
+  } catch (const std::bad_alloc&) {
+    return fail(NCORR_ERR_CAPACITY, "host memory exhausted");
+  } catch (const std::exception& e) {
+    return fail(NCORR_ERR_INVALID_ARGUMENT, e.what());
+  }
 }
 
 }  // extern "C"
