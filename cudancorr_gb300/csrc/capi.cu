@@ -699,41 +699,64 @@ static void gauss_legendre(int n, std::vector<double>& x, std::vector<double>& w
   }
 }
 
+// The 48-point Gauss-Legendre rule, built once on first use (a function-local
+// static: its initialisation is thread-safe, so concurrent conversions share
+// it without a race).
+struct GaussLegendre48 {
+  std::vector<double> x, w;
+  GaussLegendre48() { gauss_legendre(48, x, w); }
+};
+static const GaussLegendre48& gl48() {
+  static const GaussLegendre48 rule;
+  return rule;
+}
+
+// Comoving distance in Mpc/h: (c/100) * integral_0^z dz' / E(z'),
+// E(z) = sqrt(OmegaM (1+z)^3 + OmegaLambda) (source/survey.cu:17-37, where
+// GSL's qags integrates to 1e-7 relative). The integral is taken in
+// u = ln(1 + z'), dz' = (1 + z') du, whose integrand (1+z)/E(z) is smooth for
+// every z > -1; 48-point Gauss-Legendre panels of width <= 0.25 in u keep
+// the error near 1e-15 relative, with at most a few dozen panels for any
+// finite z. A negative z gives the negative integral, as qags from 0 to z
+// does; z <= -1 or a non-finite z gives NaN.
+static double comoving_distance(double z, double om, double ol) {
+  constexpr double c_over_100 = 299792.458 / 100.0;  // source/survey.cu:12, :36
+  if (z == 0.0) return 0.0;
+  if (!(z > -1.0) || !std::isfinite(z)) return std::numeric_limits<double>::quiet_NaN();
+  const GaussLegendre48& gl = gl48();
+  const double umax = std::log1p(z);
+  const int panels = std::max(1, static_cast<int>(std::ceil(std::fabs(umax) / 0.25)));
+  const double hw = umax / panels / 2.0;
+  double s = 0.0;
+  for (int p = 0; p < panels; ++p) {
+    const double mid = (2 * p + 1) * hw;
+    for (size_t k = 0; k < gl.x.size(); ++k) {
+      const double a = std::exp(mid + hw * gl.x[k]);  // 1 + z'
+      s += gl.w[k] * a / std::sqrt(om * a * a * a + ol);
+    }
+  }
+  return c_over_100 * s * hw;
+}
+
 int survey_convert_coordinates(const double cosmo[3], const double* in, int64_t n, double* out) {
   if (!cosmo || n < 0 || (n > 0 && (!in || !out)))
     return fail(NCORR_ERR_INVALID_ARGUMENT, "null or negative argument");
-  const double om = cosmo[1], ol = cosmo[2];
-  const double c_over_100 = 299792.458 / 100.0;  // source/survey.cu:12, :36
-  const double deg = 3.14159265358979323846 / 180.0;
-  static std::vector<double> gx, gw;
-  static bool init = false;
-  if (!init) {
-    gauss_legendre(48, gx, gw);
-    init = true;
-  }
-  // 1/E(z) is smooth on [0, z]; 48-point Gauss-Legendre on panels of width
-  // <= 0.5 in z converges to ~1e-15 relative.
-  auto dist = [&](double z) {
-    if (!(z > 0.0)) return 0.0;
-    const int panels = std::max(1, static_cast<int>(std::ceil(z / 0.5)));
-    const double hw = z / panels / 2.0;
-    double s = 0.0;
-    for (int p = 0; p < panels; ++p) {
-      const double mid = (2 * p + 1) * hw;
-      for (size_t k = 0; k < gx.size(); ++k) {
-        const double zz = mid + hw * gx[k];
-        s += gw[k] / std::sqrt(om * std::pow(1.0 + zz, 3) + ol);
-      }
+  try {
+    const double om = cosmo[1], ol = cosmo[2];
+    const double deg = 3.14159265358979323846 / 180.0;
+    for (int64_t i = 0; i < n; ++i) {
+      const double ra = in[4 * i] * deg, dec = in[4 * i + 1] * deg, z = in[4 * i + 2], w = in[4 * i + 3];
+      const double d = comoving_distance(z, om, ol);
+      // source/survey.cu:48-50
+      out[4 * i] = d * std::cos(dec) * std::cos(ra);
+      out[4 * i + 1] = d * std::cos(dec) * std::sin(ra);
+      out[4 * i + 2] = d * std::sin(dec);
+      out[4 * i + 3] = w;
     }
-    return c_over_100 * s * hw;
-  };
-  for (int64_t i = 0; i < n; ++i) {
-    const double ra = in[4 * i] * deg, dec = in[4 * i + 1] * deg, z = in[4 * i + 2], w = in[4 * i + 3];
-    const double d = dist(z);
-    out[4 * i] = d * std::cos(dec) * std::cos(ra);
-    out[4 * i + 1] = d * std::cos(dec) * std::sin(ra);
-    out[4 * i + 2] = d * std::sin(dec);
-    out[4 * i + 3] = w;
+  } catch (const std::bad_alloc&) {
+    return fail(NCORR_ERR_CAPACITY, "host memory exhausted");
+  } catch (const std::exception& e) {
+    return fail(NCORR_ERR_INVALID_ARGUMENT, e.what());
   }
   return NCORR_OK;
 }
@@ -781,13 +804,21 @@ namespace {
 std::mutex g_noalloc_mutex;
 void* g_noalloc_ptr[kNoAllocMaxDevices] = {};
 
-// Device address of the scratch array on the current device, looked up once
-// per device (the host-side name of a __device__ array is not a device
-// address).
-int noalloc_scratch(int dev, unsigned char** out) {
+// Device address of the scratch array on the current device (the host-side
+// name of a __device__ array is not a device address). It is looked up on
+// every call made outside a stream capture, so that a device reset, after
+// which the module is loaded again, cannot leave a stale address behind; a
+// call inside a capture uses the address found by an earlier call on that
+// device, or looks it up if there is none.
+int noalloc_scratch(int dev, cudaStream_t st, unsigned char** out) {
   if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(NCORR_ERR_INVALID_ARGUMENT, "device index out of range");
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cap) != cudaSuccess) {
+    cudaGetLastError();
+    cap = cudaStreamCaptureStatusNone;
+  }
   std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (!g_noalloc_ptr[dev]) {
+  if (!g_noalloc_ptr[dev] || cap == cudaStreamCaptureStatusNone) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || !p)
@@ -800,9 +831,9 @@ int noalloc_scratch(int dev, unsigned char** out) {
 
 }  // namespace
 
-extern "C" int ncorr_count_noalloc(const double box[3], const double* edges, int n_edges, int is_survey,
-                                   const double* d_p1, int64_t n1, const double* d_p2, int64_t n2,
-                                   const double* d_p3, int64_t n3, double* d_counts_all, void* stream) {
+static int count_noalloc_impl(const double box[3], const double* edges, int n_edges, int is_survey,
+                              const double* d_p1, int64_t n1, const double* d_p2, int64_t n2, const double* d_p3,
+                              int64_t n3, double* d_counts_all, void* stream) {
   static_assert(3 * kNoAllocCatBytes + kNoAllocHistBytes + kTableSize + kNoAllocExactCap * sizeof(ExactEntry) +
                         sizeof(KArgs) + sizeof(BatchItem) + 64 * 1024 <= kNoAllocBytes,
                 "scratch layout exceeds the scratch array");
@@ -853,10 +884,10 @@ extern "C" int ncorr_count_noalloc(const double box[3], const double* edges, int
 
   int dev = 0;
   CU(cudaGetDevice(&dev));
-  unsigned char* base = nullptr;
-  if (int rc = noalloc_scratch(dev, &base)) return rc;
-  cudaGetLastError();
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  unsigned char* base = nullptr;
+  if (int rc = noalloc_scratch(dev, st, &base)) return rc;
+  cudaGetLastError();
 
   // Carve the scratch: three cell lists, histogram, table, exact queue, small
   // counters, kernel arguments.
@@ -986,33 +1017,7 @@ extern "C" int ncorr_count_noalloc(const double box[3], const double* edges, int
   // Bin table, built on the host stack and copied in (a pageable source:
   // the copy has completed when cudaMemcpyAsync returns).
   unsigned char tab_host[kTableSize];
-  {
-    const int n = kTableSize;
-    const double vmax = g.sqr_rmax * 1.05;
-    const float scale = static_cast<float>((n - 2) / vmax);
-    g.tab_scale = scale;
-    g.tab_n = n;
-    const double ka = g.ka, kb = g.kb;
-    for (int i = 0; i < n; ++i) {
-      double lo = (i - 0.5) / static_cast<double>(scale);
-      double hi = (i + 0.5) / static_cast<double>(scale);
-      if (lo < 0) lo = 0;
-      if (i == n - 1) hi = std::numeric_limits<double>::infinity();
-      const double blo = lo - (ka * lo + kb) * 1.01;
-      const double bhi = hi + (ka * hi + kb) * 1.01;
-      unsigned char code = static_cast<unsigned char>(kCodeCareful);
-      if (bhi <= g.sqr_rmin || blo >= g.sqr_rmax) {
-        code = static_cast<unsigned char>(kCodeReject);
-      } else if (blo > g.sqr_rmin && bhi < g.sqr_rmax) {
-        for (int b = 0; b < g.nb; ++b)
-          if (g.sqr_bins[b] <= blo && bhi < g.sqr_bins[b + 1]) {
-            code = static_cast<unsigned char>(b * code_scale);
-            break;
-          }
-      }
-      tab_host[i] = code;
-    }
-  }
+  build_table(g, code_scale, tab_host);
   CU(cudaMemcpyAsync(table, tab_host, kTableSize, cudaMemcpyHostToDevice, st));
   CU(cudaMemsetAsync(hist, 0, (weighted ? 2 : 1) * static_cast<size_t>(nbin) * sizeof(unsigned long long), st));
 
@@ -1074,4 +1079,17 @@ extern "C" int ncorr_count_noalloc(const double box[3], const double* edges, int
   CU(cudaStreamSynchronize(st));
   if (kflags & kFlagListOverflow) return fail(NCORR_ERR_CAPACITY, "neighbour list overflow");
   return NCORR_OK;
+}
+
+// Nothing throws across the C ABI: the mutex and the error strings may.
+extern "C" int ncorr_count_noalloc(const double box[3], const double* edges, int n_edges, int is_survey,
+                                   const double* d_p1, int64_t n1, const double* d_p2, int64_t n2,
+                                   const double* d_p3, int64_t n3, double* d_counts_all, void* stream) {
+  try {
+    return count_noalloc_impl(box, edges, n_edges, is_survey, d_p1, n1, d_p2, n2, d_p3, n3, d_counts_all, stream);
+  } catch (const std::bad_alloc&) {
+    return fail(NCORR_ERR_CAPACITY, "host memory exhausted");
+  } catch (const std::exception& e) {
+    return fail(NCORR_ERR_INVALID_ARGUMENT, e.what());
+  }
 }

@@ -239,9 +239,9 @@ inline void set_error_model(Geom& g) {
 // bin that contains the whole error band of every such v (times code_scale,
 // the byte stride of a bin in the CTA histogram), kCodeReject when the band
 // lies outside (rmin^2, rmax^2), or kCodeCareful otherwise.
-inline void build_table(Geom& g, int code_scale, std::vector<unsigned char>& tab) {
+// `tab` holds kTableSize entries.
+inline void build_table(Geom& g, int code_scale, unsigned char* tab) {
   const int n = kTableSize;
-  tab.assign(n, static_cast<unsigned char>(kCodeCareful));
   const double vmax = g.sqr_rmax * 1.05;
   const float scale = static_cast<float>((n - 2) / vmax);
   g.tab_scale = scale;
@@ -268,6 +268,11 @@ inline void build_table(Geom& g, int code_scale, std::vector<unsigned char>& tab
     }
     tab[i] = code;
   }
+}
+
+inline void build_table(Geom& g, int code_scale, std::vector<unsigned char>& tab) {
+  tab.assign(kTableSize, static_cast<unsigned char>(kCodeCareful));
+  build_table(g, code_scale, tab.data());
 }
 
 #define CU(call)                                                              \

@@ -149,6 +149,9 @@ static int random_catalog_impl(int64_t n, const double box[3], uint64_t seed, do
     }
   };
   std::vector<std::thread> pool;
+  // Reserved up front, so that starting a thread never reallocates the
+  // vector: a growth failure there would unwind past joinable threads.
+  pool.reserve(nth);
   unsigned started = 1;  // stripes handed to threads (stripe 0 runs here)
   try {
     for (unsigned t = 1; t < nth; ++t) {

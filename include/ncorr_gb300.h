@@ -205,7 +205,11 @@ int ncorr_random_catalog(int64_t n, const double box[3], uint64_t seed, double* 
  * catalogues (n x 4 doubles, 16-byte aligned); d_counts_all receives the
  * nb^3 doubles of triCountsAll_, as ncorr_get_tri_counts_all returns them.
  * The first call on each device looks up the array's device address, so make
- * it before any stream capture. Calls share the array: calls that overlap on
+ * it before any stream capture; later calls outside a capture look it up
+ * again (a device reset reloads the library's module and moves the array),
+ * calls inside a capture reuse the last address found on that device, so do
+ * not reset a device between that look-up and a captured call. Calls share
+ * the array: calls that overlap on
  * the GPU (other threads, other streams) race, so serialise them. Returns
  * after the work on `stream` (null: the legacy default stream) completes. */
 int ncorr_count_noalloc(const double box[3], const double* edges, int n_edges, int is_survey,

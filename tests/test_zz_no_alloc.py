@@ -18,7 +18,6 @@ from tests import cases
 
 pytestmark = pytest.mark.gpu
 
-WEIGHTED_RTOL = 1e-6  # the weighted-bin tolerance of the parity tests
 
 
 def regular(box, edges, p1, p2, p3, survey):
@@ -45,7 +44,9 @@ def noalloc(box, edges, t1, t2, t3, survey, out):
 def test_noalloc_matches_regular_entry_twice():
     """Two calls in a row on the same scratch: unweighted box counts (the
     six-fold symmetric loop, and the pairwise loop of a non-divisible box)
-    bit for bit, weighted survey DDR bins within tolerance."""
+    and weighted survey DDR bins, all bit for bit. The weighted sums are
+    exact fixed-point integers with the same scale on both paths, so they do
+    not depend on the order of the additions."""
     torch = pytest.importorskip("torch")
     for make in (cases.small_box_uniform, cases.small_box_nondivisible):
         p, box, edges = make()
@@ -58,14 +59,35 @@ def test_noalloc_matches_regular_entry_twice():
     d, r, sbox, _, _ = cases.small_survey(nd=3000, nr=6000, weighted=True)
     sedges = api.logspace(3.0, 40.0, 9)
     ref_w = regular(sbox, sedges, d, d, r, True)
-    nz = ref_w != 0
-    assert nz.sum() > 10
+    assert (ref_w != 0).sum() > 10
     td, tr = torch.from_numpy(d).cuda(), torch.from_numpy(r).cuda()
     out_w = torch.full(((len(sedges) - 1) ** 3,), -1.0, dtype=torch.float64, device="cuda")
     for _ in range(2):
-        h = noalloc(sbox, sedges, td, td, tr, True, out_w)
-        assert np.array_equal(h != 0, nz)
-        assert np.max(np.abs(h[nz] - ref_w[nz]) / np.abs(ref_w[nz])) < WEIGHTED_RTOL
+        assert np.array_equal(noalloc(sbox, sedges, td, td, tr, True, out_w), ref_w)
+
+
+def test_noalloc_three_catalogues_and_survey_ddd():
+    """Three distinct box catalogues (p1, p2, p3 all different), and an
+    unweighted survey DDD (the six-fold loop on the clipped grid), each twice
+    in a row, bit for bit against the regular entry point."""
+    torch = pytest.importorskip("torch")
+    p1, box, edges = cases.small_box_uniform(seed=31, n=2500)
+    p2 = C.uniform_box(2800, box, 32)
+    p3 = C.uniform_box(3100, box, 33)
+    ref = regular(box, edges, p1, p2, p3, False)
+    assert ref.sum() > 0
+    t1, t2, t3 = (torch.from_numpy(a).cuda() for a in (p1, p2, p3))
+    out = torch.full(((len(edges) - 1) ** 3,), -1.0, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        assert np.array_equal(noalloc(box, edges, t1, t2, t3, False, out), ref)
+    d, _, sbox, _, _ = cases.small_survey(nd=4000, nr=10)
+    sedges = api.logspace(3.0, 40.0, 9)
+    ref_s = regular(sbox, sedges, d, d, d, True)
+    assert ref_s.sum() > 0
+    td = torch.from_numpy(d).cuda()
+    out_s = torch.full(((len(sedges) - 1) ** 3,), -1.0, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        assert np.array_equal(noalloc(sbox, sedges, td, td, td, True, out_s), ref_s)
 
 
 def test_noalloc_rejects_dense_neighbourhoods():
@@ -94,3 +116,30 @@ def test_noalloc_rejects_oversize():
                                  ctypes.c_void_p(out.data_ptr()), None)
     assert rc == api.NCORR_ERR_CAPACITY
     assert b"65536" in lib.ncorr_last_error()
+
+
+def _raw_call(box, edges, t, out):
+    lib = api.load_library()
+    b = np.ascontiguousarray(np.broadcast_to(np.asarray(box, dtype=np.float64), (3,)))
+    e = np.ascontiguousarray(np.asarray(edges, dtype=np.float64))
+    D = ctypes.POINTER(ctypes.c_double)
+    rc = lib.ncorr_count_noalloc(b.ctypes.data_as(D), e.ctypes.data_as(D), len(e), 0,
+                                 ctypes.c_void_p(t.data_ptr()), t.shape[0], ctypes.c_void_p(t.data_ptr()),
+                                 t.shape[0], ctypes.c_void_p(t.data_ptr()), t.shape[0],
+                                 ctypes.c_void_p(out.data_ptr()), None)
+    return rc, lib.ncorr_last_error()
+
+
+def test_noalloc_rejects_cell_and_bin_limits():
+    """More than 32768 cells (33^3 here) or more than 31 bins per side is
+    refused with NCORR_ERR_CAPACITY / NCORR_ERR_INVALID_ARGUMENT and a message
+    naming the limit."""
+    torch = pytest.importorskip("torch")
+    p = C.uniform_box(1000, 330.0, 5)
+    t = torch.from_numpy(p).cuda()
+    out = torch.zeros((4 ** 3,), dtype=torch.float64, device="cuda")
+    rc, msg = _raw_call(330.0, C.linear_edges(10.0, 4), t, out)
+    assert rc == api.NCORR_ERR_CAPACITY and b"32768 cells" in msg
+    out32 = torch.zeros((32 ** 3,), dtype=torch.float64, device="cuda")
+    rc, msg = _raw_call(330.0, C.linear_edges(64.0, 32), t, out32)
+    assert rc == api.NCORR_ERR_INVALID_ARGUMENT and b"31 bins" in msg
