@@ -494,12 +494,8 @@ def survey_catalogues(seed: int):
     """Data 500k (lognormal(0, 0.3) weights) and randoms 2.5M in the RA 0-90,
     Dec 0-60 wedge, r ~ N(1000, 150) in [600, 1400], jointly shifted by the
     engine's prep_cat_survey; 15 log bins in [5, 120)."""
-    from cudancorr_gb300 import api
     from cudancorr_gb300 import catalogs as C
-    d = C.survey_wedge(500_000, seed, True)
-    r = C.survey_wedge(2_500_000, seed + 1, False)
-    box, ori = api.prep_cat_survey(d, r)
-    return d, r, box, ori, api.logspace(5.0, 120.0, 16)
+    return C.config_survey(seed)
 
 
 def run_survey(args) -> dict:

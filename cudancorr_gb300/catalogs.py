@@ -113,15 +113,37 @@ def config_soneira_peebles(seed: int = 5, n_top: int = 3906):
     return soneira_peebles(n_top, 5, 4, 1.9, 200.0, 1500.0, seed), 1500.0, linear_edges(80.0, 16)
 
 
+def batch_mock_sizes(seed: int = 4, n_mocks: int = 64, n_min: int = 50_000, n_max: int = 1_000_000):
+    """Target sizes of the batched mocks: log-uniform in [n_min, n_max]."""
+    rng = np.random.default_rng(seed)
+    return np.exp(rng.uniform(np.log(n_min), np.log(n_max), n_mocks))
+
+
+def batch_mock(i: int, size: float, seed: int = 4) -> np.ndarray:
+    """Mock i of the batch: N/8 parents x Poisson(8), sigma 1.5, L=1000."""
+    return neyman_scott(max(1, int(round(size / 8.0))), 8.0, 1.5, 1000.0, seed * 1000 + i)
+
+
 def config_batch_mocks(seed: int = 4, n_mocks: int = 64, n_min: int = 50_000, n_max: int = 1_000_000):
     """64 Neyman-Scott mocks in L=1000 with sizes log-uniform in
     [50,000, 1,000,000]: N/8 parents, Poisson(8) children, sigma 1.5;
     r_max=60 (17 cells, the last 40 wide), 12 linear bins."""
-    rng = np.random.default_rng(seed)
-    sizes = np.exp(rng.uniform(np.log(n_min), np.log(n_max), n_mocks))
-    mocks = [neyman_scott(max(1, int(round(s / 8.0))), 8.0, 1.5, 1000.0, seed * 1000 + i)
-             for i, s in enumerate(sizes)]
+    sizes = batch_mock_sizes(seed, n_mocks, n_min, n_max)
+    mocks = [batch_mock(i, s, seed) for i, s in enumerate(sizes)]
     return mocks, 1000.0, linear_edges(60.0, 12)
+
+
+def config_survey(seed: int = 7):
+    """Survey wedge: data 500,000 points with lognormal(0, 0.3) weights and
+    randoms 2,500,000 points with unit weights, RA 0-90 deg, Dec 0-60 deg,
+    r ~ N(1000, 150) in [600, 1400], jointly shifted by prep_cat_survey
+    (source/survey.cu:106-128); 15 log bins in [5, 120).
+    Returns (data, randoms, box, ori, edges)."""
+    from . import api
+    d = survey_wedge(500_000, seed, True)
+    r = survey_wedge(2_500_000, seed + 1, False)
+    box, ori = api.prep_cat_survey(d, r)
+    return d, r, box, ori, api.logspace(5.0, 120.0, 16)
 
 
 def training_soneira_peebles(index: int):

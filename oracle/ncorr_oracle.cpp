@@ -226,12 +226,20 @@ inline int triangle_index(double r1, double r2, double r3, const std::vector<dou
   float s3 = std::sqrt(static_cast<float>(r3));
   float sum = s1 + s2;
   if (sum <= s3) return -1;
-  int idx[3] = {-1, -1, -1};
+  // The reference scans every bin for each side (the last match wins); with
+  // strictly increasing edges at most one bin matches, which a binary search
+  // finds directly.
   const double r[3] = {r1, r2, r3};
-  for (int i = 0; i < nb; ++i)
-    for (int m = 0; m < 3; ++m)
-      if (r[m] >= sb[i] && r[m] < sb[i + 1]) idx[m] = i;
-  if (idx[0] < 0 || idx[1] < 0 || idx[2] < 0) return -1;
+  int idx[3];
+  for (int m = 0; m < 3; ++m) {
+    if (!(r[m] >= sb[0] && r[m] < sb[nb])) return -1;
+    int lo = 0, hi = nb - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (r[m] >= sb[mid]) lo = mid; else hi = mid - 1;
+    }
+    idx[m] = lo;
+  }
   return idx[2] + idx[1] * nb + idx[0] * nb * nb;
 }
 
@@ -364,11 +372,51 @@ void count_lists(const Geometry& g, const Pt* p1, long n1, const Grid& g2, const
   const int nb = g.nb;
   const long nbin = static_cast<long>(nb) * nb * nb;
   std::vector<std::vector<Acc>> part(nthreads, std::vector<Acc>(nbin));
+  // Row j of one anchor's pair loop. With p2 == p3 the ordered pairs (j, l)
+  // and (l, j) have bit-identical sides ((a-b)^2 == (b-a)^2, and the triangle
+  // index sorts the three), so each unordered pair is evaluated once and adds
+  // both orderings' weight products; l == j has r3 = 0, which the strict
+  // r_min test rejects.
+  auto row = [&](const Pt& q1, const std::vector<Nbr>& l2, const std::vector<Nbr>& L3, size_t j,
+                 std::vector<Acc>& h) {
+    const Nbr& b = l2[j];
+    const double w12 = q1.w * b.p.w;
+    const size_t lend = same23 ? j : L3.size();
+    for (size_t l = 0; l < lend; ++l) {
+      const Nbr& c = L3[l];
+      double r3 = sqr_sep<P>(b.p, c.p);
+      if (r3 < g.sqr_rmax && r3 > g.sqr_rmin) {
+        int t = triangle_index(b.r, c.r, r3, g.sqr_bins, nb);
+        if (t != -1) {
+          h[t].add(w12 * c.p.w);
+          if (same23) h[t].add((q1.w * c.p.w) * b.p.w);
+        }
+      }
+    }
+  };
+  if (n1 >= 8L * nthreads) {
+    // Many anchors: threads take whole anchors.
 #pragma omp parallel num_threads(nthreads)
-  {
+    {
+      std::vector<Nbr> l2, l3;
+      std::vector<Acc>& h = part[omp_get_thread_num()];
+#pragma omp for schedule(dynamic, 1)
+      for (long a = 0; a < n1; ++a) {
+        const Pt q1 = p1[a];
+        int home[3];
+        anchor_cell(g, q1, home);
+        gather<P>(g, q1, home, g2, &l2);
+        const std::vector<Nbr>* pl3 = &l2;
+        if (!same23) {
+          gather<P>(g, q1, home, g3, &l3);
+          pl3 = &l3;
+        }
+        for (size_t j = 0; j < l2.size(); ++j) row(q1, l2, *pl3, j, h);
+      }
+    }
+  } else {
+    // Few anchors: the rows of each anchor's pair loop are shared out.
     std::vector<Nbr> l2, l3;
-    std::vector<Acc>& h = part[omp_get_thread_num()];
-#pragma omp for schedule(dynamic, 4)
     for (long a = 0; a < n1; ++a) {
       const Pt q1 = p1[a];
       int home[3];
@@ -379,19 +427,9 @@ void count_lists(const Geometry& g, const Pt* p1, long n1, const Grid& g2, const
         gather<P>(g, q1, home, g3, &l3);
         pl3 = &l3;
       }
-      const std::vector<Nbr>& L3 = *pl3;
-      for (size_t j = 0; j < l2.size(); ++j) {
-        const Nbr& b = l2[j];
-        const double w12 = q1.w * b.p.w;
-        for (size_t l = 0; l < L3.size(); ++l) {
-          const Nbr& c = L3[l];
-          double r3 = sqr_sep<P>(b.p, c.p);
-          if (r3 < g.sqr_rmax && r3 > g.sqr_rmin) {
-            int t = triangle_index(b.r, c.r, r3, g.sqr_bins, nb);
-            if (t != -1) h[t].add(w12 * c.p.w);
-          }
-        }
-      }
+      const long nrow = static_cast<long>(l2.size());
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 8)
+      for (long j = 0; j < nrow; ++j) row(q1, l2, *pl3, static_cast<size_t>(j), part[omp_get_thread_num()]);
     }
   }
   out->assign(nbin, Acc());

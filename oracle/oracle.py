@@ -304,3 +304,50 @@ def reference_count_rppi(box, edges, num_pi_bins, p1, p2=None, p3=None, survey=F
     if rc != 0:
         raise RuntimeError(R.ref_runner_last_error().decode())
     return out, ov.value, kms.value, tms.value
+
+
+# ---------------------------------------------------------------- reference-kernel cost model
+def reference_cells(p, box, rmax):
+    """The reference's cell index of every point, int(x / r_max) with the
+    == nc clamp (source/cudaNcorr.cu:50-58); returns (cells, nc)."""
+    box = np.broadcast_to(np.asarray(box, dtype=np.float64), (3,))
+    nc = np.ceil(box / rmax).astype(np.int64)
+    c = (np.asarray(p)[:, :3] / rmax).astype(np.int64)
+    for d in range(3):
+        c[c[:, d] == nc[d], d] = nc[d] - 1
+    return c, nc
+
+
+def reference_n27(anchor_cells, p, box, rmax, survey):
+    """Points of catalogue p in the 27 cells around each anchor cell (wrapped
+    once in a box, clipped in a survey), as the reference's loops visit them."""
+    c, nc = reference_cells(p, box, rmax)
+    cnt = np.zeros(tuple(nc), np.int64)
+    np.add.at(cnt, (c[:, 0], c[:, 1], c[:, 2]), 1)
+    s = np.zeros_like(cnt)
+    if survey:
+        pad = np.pad(cnt, 1)
+        for dx in range(3):
+            for dy in range(3):
+                for dz in range(3):
+                    s += pad[dx:dx + nc[0], dy:dy + nc[1], dz:dz + nc[2]]
+    else:
+        for dx in (-1, 0, 1):
+            for dy in (-1, 0, 1):
+                for dz in (-1, 0, 1):
+                    s += np.roll(cnt, (dx, dy, dz), axis=(0, 1, 2))
+    a = anchor_cells
+    return s[a[:, 0], a[:, 1], a[:, 2]]
+
+
+def reference_anchor_cost(p1, p2, p3, box, rmax, survey=False):
+    """Estimated pair evaluations of the reference kernel's thread for each
+    anchor of p1 (source/device.cu:270-312: for every p2 point in the 27
+    cells in range, every p3 point in the 27 cells): (1 + k2) * n27(p3), with
+    the in-range count k2 ~ 0.155 n27(p2) (a ball's share of 27 cells).
+    Returns (cost, face) where face marks anchors in the first or last cell
+    layer of the grid."""
+    a, nc = reference_cells(p1, box, rmax)
+    cost = (1.0 + 0.155 * reference_n27(a, p2, box, rmax, survey)) * reference_n27(a, p3, box, rmax, survey)
+    face = ((a == 0) | (a == nc - 1)).any(axis=1)
+    return cost, face
