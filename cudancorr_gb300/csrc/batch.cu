@@ -54,7 +54,7 @@ struct ncorr_batch {
   DevBuf in, cid, pd, pq, pc, count, start, cursor, flags, wmax, bound;
   // Items, histograms, results and the launch's own buffers.
   DevBuf items, hist, out, total, item_off, q_item, q_anchor, s_item, s_anchor, work, stats, xq, xq_count;
-  DevBuf slab_e, slab_m, slab_p, slab_w, args, args_probe, table, feats;
+  DevBuf slab_e, slab_m, slab_p, slab_w, slab_q, slab_x, args, args_probe, table, feats;
   OrderBufs order;
   unsigned xq_cap = 0;
   // Page-locked host mirrors the graph writes.
@@ -178,25 +178,14 @@ int enqueue_count(ncorr_batch* b, bool set_attr) {
   return NCORR_OK;
 }
 
-// Launch shape for a tuning choice: histogram copies that fit, list
-// capacity, occupancy. Returns false when the kernel cannot run so.
-bool shape(ncorr_batch* b, int copies, int* ks_out, size_t* smem_out, int* grid_out) {
-  const int nb = b->h->nb;
-  const long nbin = static_cast<long>(nb) * nb * nb;
-  const int elem = b->weighted ? 8 : 4;
-  if (b->hg && copies > 1) return false;
-  if (copies > 1 && copies * nbin * elem > kHistSmemMax) return false;
-  const SmemLayout L0 = make_layout(nb, 0, b->sym, b->weighted, b->hg, copies);
-  const int per = (b->sym ? 1 : 2) * (16 + 4 + 4 + (b->weighted ? 4 : 0));
-  int ks = ((kSmemBudget - L0.total) / per / kTile) * kTile;
-  if (ks < kTile) ks = kTile;
-  const SmemLayout L = make_layout(nb, ks, b->sym, b->weighted, b->hg, copies);
-  const int occ = triangles_occupancy(b->h->survey != 0, b->sym, b->weighted, b->hg, L.total);
-  if (occ <= 0) return false;
-  *ks_out = ks;
-  *smem_out = static_cast<size_t>(L.total);
-  *grid_out = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(b->n_work, static_cast<int64_t>(b->nsm) * occ)));
-  return true;
+// Launch shape for a tuning choice (histogram copies) and the largest
+// 27-cell occupancy of any catalogue. Returns false when the kernel cannot
+// run with exactly that many copies.
+bool shape(ncorr_batch* b, int copies, int kmax, TriShape* out) {
+  if (!tri_shape(b->h->nb, b->h->survey != 0, b->sym, b->weighted, b->hg, copies, b->nsm, b->n_work, kmax, kmax,
+                 out))
+    return false;
+  return out->copies == copies;
 }
 
 int plan(ncorr_batch* b, int autotune) {
@@ -314,30 +303,37 @@ int plan(ncorr_batch* b, int autotune) {
       cudaHostAlloc(&b->h_total, b->n_items * sizeof(unsigned long long), cudaHostAllocDefault) != cudaSuccess)
     return fail(NCORR_ERR_CUDA, "cudaHostAlloc failed");
 
-  // Tuning candidates and the slabs the largest list needs under any of them.
+  // Tuning candidates (histogram copies; the flag-group height is the
+  // handle's) and the slabs the largest list needs under any of them.
   struct Cand {
-    int sub_j, copies, ks, grid;
-    size_t smem;
+    int sub_j, copies;
+    TriShape shp;
   };
   std::vector<Cand> cands;
   const int kmax = *std::max_element(bound.begin(), bound.end());
-  int kg_max = 0;
-  for (int sj : {32, 16, 8})
-    for (int cp : {1, 2, 4}) {
-      if (!autotune && (sj != h->sub_j || cp != h->hist_copies)) continue;
-      Cand c{sj, cp, 0, 0, 0};
-      if (!shape(b, cp, &c.ks, &c.smem, &c.grid)) continue;
-      cands.push_back(c);
-      kg_max = std::max(kg_max, ((std::max(0, kmax - c.ks) + kTile - 1) / kTile) * kTile);
-    }
-  if (cands.empty()) return fail(NCORR_ERR_CUDA, "triangle kernel does not fit on the device");
+  for (int cp : {1, 2, 4}) {
+    if (!autotune && cp != h->hist_copies) continue;
+    Cand c{h->sub_j, cp, TriShape()};
+    if (!shape(b, cp, kmax, &c.shp)) continue;
+    cands.push_back(c);
+  }
+  if (cands.empty()) {
+    Cand c{h->sub_j, 1, TriShape()};
+    if (!shape(b, 1, kmax, &c.shp)) return fail(NCORR_ERR_CUDA, "triangle kernel does not fit on the device");
+    cands.push_back(c);
+  }
+  size_t slab_n = 0;
   int grid_max = 0;
-  for (const Cand& c : cands) grid_max = std::max(grid_max, c.grid);
-  const size_t slab_n = static_cast<size_t>(grid_max) * 2 * std::max(kg_max, 1);
+  for (const Cand& c : cands) {
+    slab_n = std::max(slab_n, tri_slab_entries(c.shp));
+    grid_max = std::max(grid_max, c.shp.grid);
+  }
   CU(b->slab_e.ensure(slab_n * sizeof(float4)));
   CU(b->slab_m.ensure(slab_n * sizeof(unsigned)));
   CU(b->slab_p.ensure(slab_n * sizeof(int)));
   if (b->weighted) CU(b->slab_w.ensure(slab_n * sizeof(float)));
+  CU(b->slab_q.ensure(static_cast<size_t>(grid_max) * kWarps * kQueueCap * sizeof(unsigned long long)));
+  CU(b->slab_x.ensure(static_cast<size_t>(grid_max) * kWarps * 32 * sizeof(ExactEntry)));
 
   KArgs& a = b->a;
   std::memset(&a, 0, sizeof(a));
@@ -356,6 +352,8 @@ int plan(ncorr_batch* b, int autotune) {
   a.slab_m = b->slab_m.as<unsigned>();
   a.slab_p = b->slab_p.as<int>();
   a.slab_w = b->weighted ? b->slab_w.as<float>() : nullptr;
+  a.slab_q = b->slab_q.as<unsigned long long>();
+  a.slab_x = b->slab_x.as<ExactEntry>();
   a.code_scale = code_scale;
   a.wscale = b->wscale;
   a.stats = b->stats.as<unsigned long long>();
@@ -366,10 +364,10 @@ int plan(ncorr_batch* b, int autotune) {
   auto apply = [&](const Cand& c) -> int {
     a.sub_j = c.sub_j;
     a.hist_copies = c.copies;
-    a.ks = c.ks;
-    a.kg = ((std::max(0, kmax - c.ks) + kTile - 1) / kTile) * kTile;
-    b->grid = c.grid;
-    b->smem = c.smem;
+    a.kcap2 = c.shp.kcap2;
+    a.kcap3 = c.shp.kcap3;
+    b->grid = c.shp.grid;
+    b->smem = c.shp.smem;
     CU(cudaMemcpy(b->args.p, &a, sizeof(KArgs), cudaMemcpyHostToDevice));
     return NCORR_OK;
   };
@@ -463,7 +461,7 @@ void ncorr_batch_destroy(ncorr_batch* b) {
   for (DevBuf* d : {&b->in, &b->cid, &b->pd, &b->pq, &b->pc, &b->count, &b->start, &b->cursor, &b->flags, &b->wmax,
                     &b->bound, &b->items, &b->hist, &b->out, &b->total, &b->item_off, &b->q_item, &b->q_anchor,
                     &b->s_item, &b->s_anchor, &b->work, &b->stats, &b->xq, &b->xq_count, &b->slab_e, &b->slab_m,
-                    &b->slab_p, &b->slab_w, &b->args, &b->args_probe, &b->table, &b->feats})
+                    &b->slab_p, &b->slab_w, &b->slab_q, &b->slab_x, &b->args, &b->args_probe, &b->table, &b->feats})
     d->release();
   b->order.release();
   for (double* p : {b->h_out})
@@ -578,6 +576,7 @@ int ncorr_batch_run(ncorr_batch* b, void* stream) {
     if (f & kFlagOutOfGrid) return fail(NCORR_ERR_OUT_OF_GRID, "a point lies outside the cell grid of the box");
   }
   const int kf = b->h_flags[b->n_cats];
+  if (kf & kFlagSchedStall) return fail(NCORR_ERR_CUDA, "triangle kernel: histogram binding wait timed out");
   if (kf & (kFlagListOverflow | kFlagPlanStale))
     return fail(NCORR_ERR_CAPACITY, "the catalogues no longer fit the batch plan (weights or neighbourhood "
                                     "density grew): create the batch again");

@@ -125,33 +125,21 @@ int run(ncorr_handle* h, const double4_16a* d1, int n1, const double4_16a* d2, i
     h->table_scale = code_scale;
   }
 
-  // Histogram copies that fit, then the shared-memory list capacity and the
-  // overflow slabs.
-  int copies = hg ? 1 : h->hist_copies;
-  while (copies > 1 && static_cast<long>(copies) * nbin * elem > kHistSmemMax) copies >>= 1;
-  int ks = 0;
-  {
-    SmemLayout L0 = make_layout(h->nb, 0, sym, weighted, hg, copies);
-    int per = (sym ? 1 : 2) * (16 + 4 + 4 + (weighted ? 4 : 0));
-    ks = (kSmemBudget - L0.total) / per;
-    ks = (ks / kTile) * kTile;
-    if (ks < kTile) ks = kTile;
-  }
-  SmemLayout L = make_layout(h->nb, ks, sym, weighted, hg, copies);
-  const size_t smem = static_cast<size_t>(L.total);
-  int occ = triangles_occupancy(h->survey != 0, sym, weighted, hg, smem);
-  if (occ <= 0) return fail(NCORR_ERR_CUDA, "triangle kernel does not fit on the device");
+  // Launch shape (histogram copies that fit, shared memory, grid) and the
+  // per-warp slabs: neighbour lists sized by the largest 27-cell occupancy,
+  // careful queues, exact buffers.
   int nsm = 0;
   CU(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->device));
-  int grid = std::max(1, std::min(n1, nsm * occ));
-  const int kmax = std::max(bound[0], bound[1]);
-  int kg = std::max(0, kmax - ks);
-  kg = ((kg + kTile - 1) / kTile) * kTile;
-  const size_t slab_n = static_cast<size_t>(grid) * 2 * std::max(kg, 1);
+  TriShape shp;
+  if (!tri_shape(h->nb, h->survey != 0, sym, weighted, hg, h->hist_copies, nsm, n1, bound[0], bound[1], &shp))
+    return fail(NCORR_ERR_CUDA, "triangle kernel does not fit on the device");
+  const size_t slab_n = tri_slab_entries(shp);
   CU(h->slab_e.ensure(slab_n * sizeof(float4)));
   CU(h->slab_m.ensure(slab_n * sizeof(unsigned)));
   CU(h->slab_p.ensure(slab_n * sizeof(int)));
   if (weighted) CU(h->slab_w.ensure(slab_n * sizeof(float)));
+  CU(h->slab_q.ensure(static_cast<size_t>(shp.grid) * kWarps * kQueueCap * sizeof(unsigned long long)));
+  CU(h->slab_x.ensure(static_cast<size_t>(shp.grid) * kWarps * 32 * sizeof(ExactEntry)));
 
   const size_t hist_words = weighted ? 2 * static_cast<size_t>(nbin) : static_cast<size_t>(nbin);
   CU(h->d_hist.ensure(hist_words * sizeof(unsigned long long)));
@@ -185,7 +173,7 @@ int run(ncorr_handle* h, const double4_16a* d1, int n1, const double4_16a* d2, i
   a.q_anchor = nullptr;
   a.sched_static = h->sched_mode == NCORR_SCHED_STATIC ? 1 : 0;
   a.sub_j = h->sub_j;
-  a.hist_copies = copies;
+  a.hist_copies = shp.copies;
   a.cell_work = nullptr;
   const bool need_feats = h->record_work || h->sched_mode == NCORR_SCHED_LEARNED;
   if (need_feats) {
@@ -217,8 +205,10 @@ int run(ncorr_handle* h, const double4_16a* d1, int n1, const double4_16a* d2, i
   a.slab_m = h->slab_m.as<unsigned>();
   a.slab_p = h->slab_p.as<int>();
   a.slab_w = weighted ? h->slab_w.as<float>() : nullptr;
-  a.ks = ks;
-  a.kg = kg;
+  a.slab_q = h->slab_q.as<unsigned long long>();
+  a.slab_x = h->slab_x.as<ExactEntry>();
+  a.kcap2 = shp.kcap2;
+  a.kcap3 = shp.kcap3;
   a.code_scale = code_scale;
   a.wscale = wscale;
   a.stats = h->d_stats.as<unsigned long long>();
@@ -235,7 +225,7 @@ int run(ncorr_handle* h, const double4_16a* d1, int n1, const double4_16a* d2, i
   a.self = h->d_args.as<KArgs>();
   CU(cudaMemcpyAsync(h->d_args.p, &a, sizeof(KArgs), cudaMemcpyHostToDevice, st));
   CU(cudaEventRecord(h->ev[2], st));
-  if (n1 > 0) CU(launch_triangles(a, h->survey != 0, sym, weighted, hg, grid, smem, st));
+  if (n1 > 0) CU(launch_triangles(a, h->survey != 0, sym, weighted, hg, shp.grid, shp.smem, st));
   if (n1 > 0) launch_exact(a, h->survey != 0, weighted, nsm * 4, st);
   CU(cudaEventRecord(h->ev[3], st));
   launch_fold(a.items, 1, h->nb, weighted, sym, 1.0 / wscale, st);
@@ -263,6 +253,7 @@ int run(ncorr_handle* h, const double4_16a* d1, int n1, const double4_16a* d2, i
   CU(cudaEventRecord(ev_end, st));
   CU(cudaStreamSynchronize(st));
   if (kflags & kFlagListOverflow) return fail(NCORR_ERR_CAPACITY, "neighbour list overflow");
+  if (kflags & kFlagSchedStall) return fail(NCORR_ERR_CUDA, "triangle kernel: histogram binding wait timed out");
   float ms0 = 0, ms1 = 0, ms2 = 0;
   cudaEventElapsedTime(&ms0, h->ev[0], h->ev[1]);
   cudaEventElapsedTime(&ms1, h->ev[2], h->ev[3]);
@@ -285,8 +276,8 @@ int run(ncorr_handle* h, const double4_16a* d1, int n1, const double4_16a* d2, i
   s.triangles = weighted ? 0 : total;
   s.weighted = weighted ? 1 : 0;
   s.symmetric = sym6 ? 6 : (sym ? 2 : 1);
-  s.grid_ctas = grid;
-  s.list_capacity = ks;
+  s.grid_ctas = shp.grid;
+  s.list_capacity = shp.kcap2;
   return NCORR_OK;
 }
 
@@ -458,7 +449,7 @@ void ncorr_destroy(ncorr_handle* h) {
   }
   for (DevBuf* b : {&h->d_table, &h->d_flags, &h->d_wmax, &h->d_work, &h->d_bound, &h->d_hist,
                     &h->d_out, &h->d_stats, &h->d_total, &h->slab_e, &h->slab_m, &h->slab_p,
-                    &h->slab_w, &h->xq, &h->xq_count, &h->d_args, &h->d_items, &h->d_cell_work,
+                    &h->slab_w, &h->slab_q, &h->slab_x, &h->xq, &h->xq_count, &h->d_args, &h->d_items, &h->d_cell_work,
                     &h->d_feats, &h->q_item, &h->q_anchor, &h->rp_pos, &h->rp_ab, &h->rp_rel, &h->rp_meta})
     b->release();
   h->order.release();
@@ -889,8 +880,16 @@ static int count_noalloc_impl(const double box[3], const double* edges, int n_ed
   if (int rc = noalloc_scratch(dev, st, &base)) return rc;
   cudaGetLastError();
 
-  // Carve the scratch: three cell lists, histogram, table, exact queue, small
-  // counters, kernel arguments.
+  // Distinct catalogues (same pointer and size: gridded once).
+  int role[3];
+  role[0] = 0;
+  role[1] = (d_p2 == d_p1 && n2 == n1) ? 0 : 1;
+  role[2] = (d_p3 == d_p2 && n3 == n2) ? role[1] : ((d_p3 == d_p1 && n3 == n1) ? 0 : 2);
+  const bool sym = role[1] == role[2];
+
+  // Carve the scratch: the distinct catalogues' cell lists (by their sizes),
+  // histogram, table, exact queue, small counters, kernel arguments; the
+  // rest holds the triangle kernel's per-warp slabs.
   size_t off = 0;
   auto take = [&](size_t bytes) {
     unsigned char* p = base + off;
@@ -902,21 +901,22 @@ static int count_noalloc_impl(const double box[3], const double* edges, int n_ed
     double4_16a* pd;
     float4* pq;
   } cat[3];
-  for (auto& c : cat) {
-    unsigned char* b = take(kNoAllocCatBytes);
-    size_t o = 0;
-    auto sub = [&](size_t bytes) {
-      unsigned char* p = b + o;
-      o += (bytes + 15) & ~size_t(15);
-      return p;
-    };
-    c.pd = reinterpret_cast<double4_16a*>(sub(kNoAllocPoints * 32));
-    c.pq = reinterpret_cast<float4*>(sub(kNoAllocPoints * 16));
-    c.cid = reinterpret_cast<int*>(sub(kNoAllocPoints * 4));
-    c.pc = reinterpret_cast<int*>(sub(kNoAllocPoints * 4));
-    c.count = reinterpret_cast<int*>(sub(kNoAllocCells * 4));
-    c.start = reinterpret_cast<int*>(sub((kNoAllocCells + 1) * 4));
-    c.cursor = reinterpret_cast<int*>(sub(kNoAllocCells * 4));
+  {
+    bool carved[3] = {false, false, false};
+    for (int r = 0; r < 3; ++r) {
+      const int ci = role[r];
+      if (carved[ci]) continue;
+      carved[ci] = true;
+      CatScratch& c = cat[ci];
+      const size_t n = static_cast<size_t>(std::max<int64_t>(ns[r], 1));
+      c.pd = reinterpret_cast<double4_16a*>(take(n * 32));
+      c.pq = reinterpret_cast<float4*>(take(n * 16));
+      c.cid = reinterpret_cast<int*>(take(n * 4));
+      c.pc = reinterpret_cast<int*>(take(n * 4));
+      c.count = reinterpret_cast<int*>(take(ncell * 4));
+      c.start = reinterpret_cast<int*>(take((ncell + 1) * 4));
+      c.cursor = reinterpret_cast<int*>(take(ncell * 4));
+    }
   }
   unsigned long long* hist = reinterpret_cast<unsigned long long*>(take(kNoAllocHistBytes));
   unsigned char* table = take(kTableSize);
@@ -930,8 +930,8 @@ static int count_noalloc_impl(const double box[3], const double* edges, int n_ed
   unsigned long long* stats = reinterpret_cast<unsigned long long*>(take(8 * sizeof(unsigned long long)));
   unsigned long long* total = reinterpret_cast<unsigned long long*>(take(sizeof(unsigned long long)));
   unsigned* xq_count = reinterpret_cast<unsigned*>(take(sizeof(unsigned)));
-  unsigned char* slab = take(256);  // the lists never overflow here (checked below)
   if (off > kNoAllocBytes) return fail(NCORR_ERR_CAPACITY, "scratch layout exceeds the scratch array");
+  const size_t slab_bytes = kNoAllocBytes - off;
 
   // Everything read before being written starts at zero on every call: the
   // array keeps the previous call's contents.
@@ -943,12 +943,6 @@ static int count_noalloc_impl(const double box[3], const double* edges, int n_ed
   CU(cudaMemsetAsync(work, 0, sizeof(int), st));
   CU(cudaMemsetAsync(xq_count, 0, sizeof(unsigned), st));
 
-  // Distinct catalogues (same pointer and size: gridded once).
-  int role[3];
-  role[0] = 0;
-  role[1] = (d_p2 == d_p1 && n2 == n1) ? 0 : 1;
-  role[2] = (d_p3 == d_p2 && n3 == n2) ? role[1] : ((d_p3 == d_p1 && n3 == n1) ? 0 : 2);
-  const bool sym = role[1] == role[2];
   bool done[3] = {false, false, false};
   for (int r = 0; r < 3; ++r) {
     const int ci = role[r];
@@ -997,22 +991,35 @@ static int count_noalloc_impl(const double box[3], const double* edges, int n_ed
   const int elem = weighted ? 8 : 4;
   const bool hg = static_cast<long>(nbin) * elem > kHistSmemMax || g.nb * elem > 0xFD;
   const int code_scale = hg ? 1 : elem;
-  int ks = 0;
-  {
-    SmemLayout L0 = make_layout(g.nb, 0, sym, weighted, hg);
-    const int per = (sym ? 1 : 2) * (16 + 4 + 4 + (weighted ? 4 : 0));
-    ks = ((kSmemBudget - L0.total) / per / kTile) * kTile;
-    if (ks < kTile) ks = kTile;
-  }
-  if (std::max(hbound[0], hbound[1]) > ks)
-    return fail(NCORR_ERR_CAPACITY, "ncorr_count_noalloc: neighbourhoods too dense for its fixed lists");
-  const SmemLayout L = make_layout(g.nb, ks, sym, weighted, hg);
-  const size_t smem = static_cast<size_t>(L.total);
-  const int occ = triangles_occupancy(g.survey != 0, sym, weighted, hg, smem);
-  if (occ <= 0) return fail(NCORR_ERR_CUDA, "triangle kernel does not fit on the device");
+  // Launch shape; the grid shrinks until the per-warp slabs (lists sized by
+  // the largest 27-cell occupancy, careful queues, exact buffers) fit the
+  // part of the scratch left after the fixed buffers.
   int nsm = 0;
   CU(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  const int grid = std::max(1, std::min(static_cast<int>(n1), nsm * occ));
+  TriShape shp;
+  if (!tri_shape(g.nb, g.survey != 0, sym, weighted, hg, 1, nsm, n1, hbound[0], hbound[1], &shp))
+    return fail(NCORR_ERR_CUDA, "triangle kernel does not fit on the device");
+  const size_t per_warp_entries = static_cast<size_t>(shp.kcap2) + shp.kcap3;
+  const size_t per_cta = kWarps * (per_warp_entries * (sizeof(float4) + sizeof(unsigned) + sizeof(int) +
+                                                       sizeof(float)) +
+                                   kQueueCap * sizeof(unsigned long long) + 32 * sizeof(ExactEntry));
+  // Six 256-byte roundings of the slab arrays, at most.
+  const size_t usable = slab_bytes > 6 * 256 ? slab_bytes - 6 * 256 : 0;
+  const int fit = static_cast<int>(std::min<size_t>(usable / per_cta, static_cast<size_t>(shp.grid)));
+  if (fit < 1)
+    return fail(NCORR_ERR_CAPACITY, "ncorr_count_noalloc: neighbourhoods too dense for its fixed scratch");
+  shp.grid = fit;
+  const size_t slab_n = tri_slab_entries(shp);
+  float4* slab_e = reinterpret_cast<float4*>(take(slab_n * sizeof(float4)));
+  unsigned* slab_m = reinterpret_cast<unsigned*>(take(slab_n * sizeof(unsigned)));
+  int* slab_p = reinterpret_cast<int*>(take(slab_n * sizeof(int)));
+  float* slab_w = reinterpret_cast<float*>(take(slab_n * sizeof(float)));
+  unsigned long long* slab_q = reinterpret_cast<unsigned long long*>(
+      take(static_cast<size_t>(shp.grid) * kWarps * kQueueCap * sizeof(unsigned long long)));
+  ExactEntry* slab_x =
+      reinterpret_cast<ExactEntry*>(take(static_cast<size_t>(shp.grid) * kWarps * 32 * sizeof(ExactEntry)));
+  if (off > kNoAllocBytes)
+    return fail(NCORR_ERR_CAPACITY, "ncorr_count_noalloc: neighbourhoods too dense for its fixed scratch");
 
   // Bin table, built on the host stack and copied in (a pageable source:
   // the copy has completed when cudaMemcpyAsync returns).
@@ -1050,16 +1057,18 @@ static int count_noalloc_impl(const double box[3], const double* edges, int n_ed
   a.n_items = 1;
   a.n_work = static_cast<int>(n1);
   a.sub_j = kSubJDefault;
-  a.hist_copies = 1;
+  a.hist_copies = shp.copies;
   a.table = table;
   a.work = work;
   a.flags = flags + 4;
-  a.slab_e = reinterpret_cast<float4*>(slab);
-  a.slab_m = reinterpret_cast<unsigned*>(slab);
-  a.slab_p = reinterpret_cast<int*>(slab);
-  a.slab_w = weighted ? reinterpret_cast<float*>(slab) : nullptr;
-  a.ks = ks;
-  a.kg = 0;
+  a.slab_e = slab_e;
+  a.slab_m = slab_m;
+  a.slab_p = slab_p;
+  a.slab_w = weighted ? slab_w : nullptr;
+  a.slab_q = slab_q;
+  a.slab_x = slab_x;
+  a.kcap2 = shp.kcap2;
+  a.kcap3 = shp.kcap3;
   a.code_scale = code_scale;
   a.wscale = wscale;
   a.stats = stats;
@@ -1069,7 +1078,7 @@ static int count_noalloc_impl(const double box[3], const double* edges, int n_ed
   a.self = d_args;
   CU(cudaMemcpyAsync(d_args, &a, sizeof(KArgs), cudaMemcpyHostToDevice, st));
   if (n1 > 0) {
-    CU(launch_triangles(a, g.survey != 0, sym, weighted, hg, grid, smem, st));
+    CU(launch_triangles(a, g.survey != 0, sym, weighted, hg, shp.grid, shp.smem, st));
     launch_exact(a, g.survey != 0, weighted, nsm * 4, st);
   }
   launch_fold(d_item, 1, g.nb, weighted, sym, 1.0 / wscale, st);
@@ -1078,6 +1087,7 @@ static int count_noalloc_impl(const double box[3], const double* edges, int n_ed
   CU(cudaMemcpyAsync(&kflags, flags + 4, sizeof(int), cudaMemcpyDeviceToHost, st));
   CU(cudaStreamSynchronize(st));
   if (kflags & kFlagListOverflow) return fail(NCORR_ERR_CAPACITY, "neighbour list overflow");
+  if (kflags & kFlagSchedStall) return fail(NCORR_ERR_CUDA, "triangle kernel: histogram binding wait timed out");
   return NCORR_OK;
 }
 

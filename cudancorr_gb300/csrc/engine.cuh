@@ -16,10 +16,10 @@
 namespace ncorr_gb300 {
 
 constexpr int kMaxEdges = 128;   // nb <= 127
-constexpr int kThreads = 256;    // triangle kernel CTA
+constexpr int kThreads = 512;    // triangle kernel CTA (one per SM)
 constexpr int kWarps = kThreads / 32;
 constexpr int kReg = 4;          // list entries per lane held in registers
-constexpr int kTile = 32 * kReg; // tile edge of the pair loop
+constexpr int kTile = 32 * kReg; // column tile of the pair loop
 constexpr int kQueueCap = 256;   // per-warp queue of careful/exact-path candidates
 #ifndef NCORR_TABLE_SIZE
 #define NCORR_TABLE_SIZE 32768
@@ -37,6 +37,7 @@ constexpr int kFlagSurveyFace = 4;    // survey anchor whose unclamped cell inde
 constexpr int kFlagListOverflow = 8;  // neighbour list exceeded its slab (host bug)
 constexpr int kFlagWeighted = 16;     // some weight != 1.0 (informational)
 constexpr int kFlagNoSym6 = 32;       // a point near a cell face or with an inexact +-box image
+constexpr int kFlagSchedStall = 128;  // a warp waited too long for the CTA histogram (never expected)
 
 struct Geom {
   int nb;                 // bins per side

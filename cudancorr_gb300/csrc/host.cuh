@@ -53,10 +53,10 @@ constexpr int kDefaultFmaPattern = 2;
 constexpr int kDefaultRpPattern = 2;
 constexpr int kDefaultDotPattern = 2;
 
-// Budget of dynamic shared memory per CTA so that two CTAs share an SM, and
-// the largest CTA histogram kept in shared memory.
-constexpr int kSmemBudget = 110 * 1024;
-constexpr long kHistSmemMax = 56 * 1024;
+// The largest histogram (all copies) the triangle kernel keeps in shared
+// memory; what the kernel leaves of the SM's 256 KB serves as L1 for the
+// neighbour lists.
+constexpr long kHistSmemMax = 96 * 1024;
 constexpr unsigned kExactQueueCap = 1u << 24;  // 16M entries, 256 MiB
 
 struct DevBuf {
@@ -142,7 +142,7 @@ struct ncorr_handle {
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   ncorr_host::CatDev cat[3];
   ncorr_host::DevBuf d_table, d_flags, d_wmax, d_work, d_bound, d_hist, d_out, d_stats, d_total;
-  ncorr_host::DevBuf slab_e, slab_m, slab_p, slab_w;
+  ncorr_host::DevBuf slab_e, slab_m, slab_p, slab_w, slab_q, slab_x;
   ncorr_host::DevBuf xq, xq_count;  // deferred exact candidates
   ncorr_host::DevBuf d_args;        // global copy of the triangle kernel's arguments
   unsigned xq_cap = 0;
@@ -273,6 +273,42 @@ inline void build_table(Geom& g, int code_scale, unsigned char* tab) {
 inline void build_table(Geom& g, int code_scale, std::vector<unsigned char>& tab) {
   tab.assign(kTableSize, static_cast<unsigned char>(kCodeCareful));
   build_table(g, code_scale, tab.data());
+}
+
+// Launch shape of the triangle kernel: histogram copies that fit (at most
+// `copies`), dynamic shared memory, persistent grid (one CTA of kWarps warps
+// per SM and resident slot, fewer for small queues), and the per-warp list
+// capacities (kcap2 for p2, kcap3 for p3 or 0 when p2 == p3), from the
+// largest 27-cell occupancies bound2/bound3.
+struct TriShape {
+  int copies = 1;
+  size_t smem = 0;
+  int grid = 0;
+  int kcap2 = 0, kcap3 = 0;
+};
+
+inline bool tri_shape(int nb, bool survey, bool sym, bool weighted, bool hg, int copies, int nsm, int64_t n_work,
+                      int bound2, int bound3, TriShape* out) {
+  const long nbin = static_cast<long>(nb) * nb * nb;
+  const int elem = weighted ? 8 : 4;
+  if (hg) copies = 1;
+  copies = std::max(1, copies);
+  while (copies > 1 && static_cast<long>(copies) * nbin * elem > kHistSmemMax) copies >>= 1;
+  const SmemLayout L = make_layout(nb, weighted, hg, copies);
+  const int occ = triangles_occupancy(survey, sym, weighted, hg, static_cast<size_t>(L.total));
+  if (occ <= 0) return false;
+  out->copies = copies;
+  out->smem = static_cast<size_t>(L.total);
+  const int64_t ctas_needed = std::max<int64_t>(1, (n_work + kWarps - 1) / kWarps);
+  out->grid = static_cast<int>(std::min<int64_t>(static_cast<int64_t>(nsm) * occ, ctas_needed));
+  out->kcap2 = ((std::max(bound2, 1) + 31) / 32) * 32;
+  out->kcap3 = sym ? 0 : ((std::max(bound3, 1) + 31) / 32) * 32;
+  return true;
+}
+
+// Entries of the per-warp list slabs of a launch.
+inline size_t tri_slab_entries(const TriShape& s) {
+  return static_cast<size_t>(s.grid) * kWarps * (static_cast<size_t>(s.kcap2) + s.kcap3);
 }
 
 #define CU(call)                                                              \

@@ -65,7 +65,7 @@ typedef struct ncorr_stats {
                               2 (p2 == p3: pairs j<l), 6 (p1 == p2 == p3 in a geometry
                               where all three vertices see each other identically) */
   int grid_ctas;           /* persistent CTAs of the triangle kernel */
-  int list_capacity;       /* shared-memory neighbour-list capacity */
+  int list_capacity;       /* per-warp neighbour-list capacity (entries, global memory) */
   double overflow;         /* rppi: count (or weight) of triangles whose reference index lies
                               past triCountsAll_ (pi bin numMinorBins from FP32 rounding);
                               the reference writes those out of bounds */
@@ -200,8 +200,10 @@ int ncorr_random_catalog(int64_t n, const double box[3], uint64_t seed, double* 
  * cudaFree would synchronise the device and stall work queued by others. All
  * working memory is one 16 MiB array inside the library, held by every GPU
  * that loads it until the process exits; limits: at most 65536 points per
- * catalogue, 32768 cells, 31 bins per side, and neighbourhoods that fit the
- * kernel's on-chip lists (NCORR_ERR_CAPACITY otherwise). Inputs are device
+ * catalogue, 32768 cells, 31 bins per side, and neighbourhoods whose lists
+ * fit the part of the array left after the catalogues' cell lists, for at
+ * least one CTA of the triangle kernel (NCORR_ERR_CAPACITY otherwise; fewer
+ * CTAs run when not all fit). Inputs are device
  * catalogues (n x 4 doubles, 16-byte aligned); d_counts_all receives the
  * nb^3 doubles of triCountsAll_, as ncorr_get_tri_counts_all returns them.
  * The first call on each device looks up the array's device address, so make
@@ -234,8 +236,10 @@ typedef struct ncorr_sched ncorr_sched;
  * alive while h uses it. */
 int ncorr_set_schedule(ncorr_handle* h, int mode, const ncorr_sched* model);
 
-/* Tuning of later calls: j-entries per work item (8, 16 or 32) and copies of
- * each CTA histogram (1, 2 or 4). The results do not depend on them. */
+/* Tuning of later calls: rows per careful-flag group of the pair loop (8, 16
+ * or 32; the uncertain candidates of a group are queued together) and copies
+ * of each CTA histogram (1, 2 or 4, as many as fit in shared memory). The
+ * results do not depend on them. */
 int ncorr_set_tuning(ncorr_handle* h, int sub_j, int hist_copies);
 
 /* When on, later calls record for each cell of the grid its 28 scheduler

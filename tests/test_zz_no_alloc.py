@@ -90,15 +90,22 @@ def test_noalloc_three_catalogues_and_survey_ddd():
         assert np.array_equal(noalloc(sbox, sedges, td, td, td, True, out_s), ref_s)
 
 
-def test_noalloc_rejects_dense_neighbourhoods():
-    """A neighbourhood larger than the on-chip lists is refused with a clear
-    error (the regular entry point spills such lists to global memory)."""
+def test_noalloc_dense_neighbourhoods():
+    """A clustered box whose neighbourhoods hold thousands of points counts
+    bit for bit like the regular entry point, twice in a row; one whose lists
+    cannot fit the fixed scratch even for one CTA (all 40,000 points in one
+    cell, seen through 27 images) is refused with a clear error."""
     torch = pytest.importorskip("torch")
     p, box, edges = cases.small_box_clustered()
+    ref = regular(box, edges, p, p, p, False)
     t = torch.from_numpy(p).cuda()
-    out = torch.zeros(((len(edges) - 1) ** 3,), dtype=torch.float64, device="cuda")
+    out = torch.full(((len(edges) - 1) ** 3,), -1.0, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        assert np.array_equal(noalloc(box, edges, t, t, t, False, out), ref)
+    q = C.uniform_box(40000, 50.0, 9)
+    tq = torch.from_numpy(q).cuda()
     with pytest.raises(AssertionError, match="too dense"):
-        noalloc(box, edges, t, t, t, False, out)
+        noalloc(50.0, edges, tq, tq, tq, False, out)
 
 
 def test_noalloc_rejects_oversize():
