@@ -46,12 +46,14 @@ EXPORTS = (
     "ncorr_set_schedule", "ncorr_set_tuning", "ncorr_set_record_work", "ncorr_num_cells",
     "ncorr_get_cell_work", "ncorr_sched_create", "ncorr_sched_destroy", "ncorr_sched_num_params",
     "ncorr_sched_get_params", "ncorr_sched_set_params", "ncorr_sched_predict", "ncorr_sched_gradient",
+    "ncorr_sched_set_precision",
     "ncorr_sched_train", "ncorr_batch_create", "ncorr_batch_run", "ncorr_batch_get_counts_all",
     "ncorr_batch_get_stats", "ncorr_batch_destroy",
 )
 
 # Work-queue schedules (ncorr_set_schedule).
 SCHED_DYNAMIC, SCHED_STATIC, SCHED_LEARNED = 0, 1, 2
+MLP_FP32, MLP_BF16 = 0, 1
 
 
 class NcorrError(RuntimeError):
@@ -150,6 +152,7 @@ def load_library() -> ctypes.CDLL:
         "ncorr_sched_get_params": (i32, [vp, _F, i64]),
         "ncorr_sched_set_params": (i32, [vp, _F, i64]),
         "ncorr_sched_predict": (i32, [vp, _F, i64, _F]),
+        "ncorr_sched_set_precision": (i32, [vp, i32]),
         "ncorr_sched_gradient": (i32, [vp, _F, _F, i64, _F, _F]),
         "ncorr_sched_train": (i32, [vp, _F, _F, i64, i32, i32, ctypes.c_float, ctypes.c_uint64, _F]),
         "ncorr_batch_create": (i32, [vp, i32, ctypes.POINTER(vp), ctypes.POINTER(i64), ctypes.POINTER(vp),
@@ -386,6 +389,11 @@ class WorkModel:
     def set_params(self, p) -> None:
         a = np.ascontiguousarray(np.asarray(p, dtype=np.float32))
         _check(self._lib.ncorr_sched_set_params(self._s, a.ctypes.data_as(_F), a.size))
+
+    def set_precision(self, precision: int) -> None:
+        """MLP_FP32 (default) or MLP_BF16: the arithmetic of the forward pass in
+        prediction, in the learned queue and in training."""
+        _check(self._lib.ncorr_sched_set_precision(self._s, int(precision)))
 
     def predict(self, feats) -> np.ndarray:
         x = np.ascontiguousarray(np.asarray(feats, dtype=np.float32).reshape(-1, 28))

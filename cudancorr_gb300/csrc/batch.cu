@@ -136,7 +136,8 @@ int enqueue_queue(ncorr_batch* b) {
     CU(b->order.ensure(b->n_items, b->h->ncell, &os));
     const int m = b->n_items * static_cast<int>(b->h->ncell);
     launch_cell_features(b->items.as<BatchItem>(), b->n_items, b->g, b->feats.as<float>(), s);
-    launch_mlp_predict(b->h->sched_model->params.as<float>(), b->feats.as<float>(), m, os.pred, s);
+    launch_mlp_predict(b->h->sched_model->params.as<float>(), b->feats.as<float>(), m, os.pred, s,
+                       b->h->sched_model->bf16);
     launch_learned_queue(b->items.as<BatchItem>(), b->n_items, static_cast<int>(b->h->ncell), os,
                          b->q_item.as<int>(), b->q_anchor.as<int>(), s);
   } else {

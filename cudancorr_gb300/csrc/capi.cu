@@ -187,7 +187,7 @@ int run(ncorr_handle* h, const double4_16a* d1, int n1, const double4_16a* d2, i
     CU(h->q_item.ensure(static_cast<size_t>(n1) * sizeof(int)));
     CU(h->q_anchor.ensure(static_cast<size_t>(n1) * sizeof(int)));
     launch_mlp_predict(h->sched_model->params.as<float>(), h->d_feats.as<float>(), static_cast<int>(h->ncell),
-                       os.pred, st);
+                       os.pred, st, h->sched_model->bf16);
     launch_learned_queue(a.items, 1, static_cast<int>(h->ncell), os, h->q_item.as<int>(), h->q_anchor.as<int>(),
                          st);
     a.q_item = h->q_item.as<int>();

@@ -171,6 +171,7 @@ struct ncorr_sched {
   int device = 0;
   cudaStream_t stream = nullptr;
   int step = 0;  // Adam steps taken
+  bool bf16 = false;  // BF16 forward pass in prediction and training
   ncorr_host::DevBuf params, m, v, grad, loss, partial, partial_loss, feats, target, idx, pred;
 };
 

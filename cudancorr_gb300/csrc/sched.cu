@@ -1,8 +1,10 @@
 // Learned scheduling: per-cell features, the work-prediction MLP (inference,
-// gradient and Adam kernels, FP32 on the CUDA cores -- 6,081 parameters are
-// far too few to feed a tensor core), and the construction of the triangle
-// kernel's work queue.
+// gradient and Adam kernels on the CUDA cores -- 6,081 parameters are far too
+// few to feed a tensor core -- in FP32, or with a BF16 forward pass), and the
+// construction of the triangle kernel's work queue.
 #include <cmath>
+
+#include <cuda_bf16.h>
 
 #include "sched.cuh"
 
@@ -51,51 +53,84 @@ void launch_cell_features(const BatchItem* items, int n_items, const Geom& g, fl
 }
 
 // ---------------------------------------------------------------------------
-// Inference: one thread per sample, parameters in shared memory.
+// BF16 forward pass: weights, inputs and hidden activations are rounded to
+// bfloat16 (round to nearest even); products of two bfloat16 values are exact
+// in FP32 and are accumulated in FP32, as a BF16 tensor-core MMA accumulates;
+// biases stay FP32. The FP32 variant uses the values unrounded.
+template <bool BF16>
+__device__ __forceinline__ float mlp_round(float x) {
+  return BF16 ? __bfloat162float(__float2bfloat16_rn(x)) : x;
+}
+
+// Inference: one thread per sample, parameters in shared memory (bfloat16
+// weights in the BF16 variant, half the bytes).
+template <bool BF16>
 __global__ void __launch_bounds__(128) k_mlp_predict(const float* __restrict__ params,
                                                      const float* __restrict__ feats, int n,
                                                      float* __restrict__ pred) {
-  __shared__ float P[kMlpParams];
-  for (int i = threadIdx.x; i < kMlpParams; i += blockDim.x) P[i] = params[i];
+  using W = typename std::conditional<BF16, __nv_bfloat16, float>::type;
+  __shared__ W Pw[kMlpOffB3 + 1];
+  __shared__ float Pb[kMlpParams];
+  for (int i = threadIdx.x; i < kMlpParams; i += blockDim.x) {
+    const float v = params[i];
+    Pb[i] = v;
+    if (BF16)
+      Pw[i] = static_cast<W>(__float2bfloat16_rn(v));
+    else
+      Pw[i] = static_cast<W>(v);
+  }
   __syncthreads();
+  auto wt = [&](int i) -> float {
+    if constexpr (BF16)
+      return __bfloat162float(Pw[i]);
+    else
+      return Pw[i];
+  };
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
   float x[kMlpIn];
 #pragma unroll
-  for (int k = 0; k < kMlpIn; ++k) x[k] = feats[static_cast<size_t>(s) * kMlpIn + k];
+  for (int k = 0; k < kMlpIn; ++k) x[k] = mlp_round<BF16>(feats[static_cast<size_t>(s) * kMlpIn + k]);
   float h1[kMlpHidden];
 #pragma unroll
   for (int i = 0; i < kMlpHidden; ++i) {
-    float a = P[kMlpOffB1 + i];
+    float a = Pb[kMlpOffB1 + i];
 #pragma unroll
-    for (int k = 0; k < kMlpIn; ++k) a = fmaf(x[k], P[kMlpOffW1 + k * kMlpHidden + i], a);
-    h1[i] = fmaxf(a, 0.0f);
+    for (int k = 0; k < kMlpIn; ++k) a = fmaf(x[k], wt(kMlpOffW1 + k * kMlpHidden + i), a);
+    h1[i] = mlp_round<BF16>(fmaxf(a, 0.0f));
   }
-  float y = P[kMlpOffB3];
+  float y = Pb[kMlpOffB3];
   for (int o = 0; o < kMlpHidden; ++o) {
-    float a = P[kMlpOffB2 + o];
+    float a = Pb[kMlpOffB2 + o];
 #pragma unroll
-    for (int i = 0; i < kMlpHidden; ++i) a = fmaf(h1[i], P[kMlpOffW2 + i * kMlpHidden + o], a);
-    y = fmaf(P[kMlpOffW3 + o], fmaxf(a, 0.0f), y);
+    for (int i = 0; i < kMlpHidden; ++i) a = fmaf(h1[i], wt(kMlpOffW2 + i * kMlpHidden + o), a);
+    y = fmaf(wt(kMlpOffW3 + o), mlp_round<BF16>(fmaxf(a, 0.0f)), y);
   }
   pred[s] = y;
 }
 
-void launch_mlp_predict(const float* params, const float* feats, int n, float* pred, cudaStream_t st) {
+void launch_mlp_predict(const float* params, const float* feats, int n, float* pred, cudaStream_t st, bool bf16) {
   if (n <= 0) return;
-  k_mlp_predict<<<(n + 127) / 128, 128, 0, st>>>(params, feats, n, pred);
+  if (bf16)
+    k_mlp_predict<true><<<(n + 127) / 128, 128, 0, st>>>(params, feats, n, pred);
+  else
+    k_mlp_predict<false><<<(n + 127) / 128, 128, 0, st>>>(params, feats, n, pred);
 }
 
 // ---------------------------------------------------------------------------
 // Gradient of the mean squared error over a minibatch. Each CTA takes
 // kMlpTile samples, runs forward and backward as small matrix products in
 // shared memory, and writes its partial gradient; partials are summed in
-// CTA order afterwards, so the result does not depend on timing.
+// CTA order afterwards, so the result does not depend on timing. In the BF16
+// variant the forward pass rounds weights, inputs and activations to
+// bfloat16 (the backward pass uses those rounded values, in FP32); the master
+// parameters and Adam stay FP32.
 constexpr int kMlpParamsPad = (kMlpParams + 3) & ~3;
 constexpr int kGradSmemFloats = kMlpParamsPad + kMlpTile * kMlpIn + 4 * kMlpTile * kMlpHidden + kMlpTile;
 
 size_t mlp_grad_smem_bytes() { return static_cast<size_t>(kGradSmemFloats) * sizeof(float); }
 
+template <bool BF16>
 __global__ void __launch_bounds__(256) k_mlp_grad(const float* __restrict__ params,
                                                   const float* __restrict__ feats,
                                                   const float* __restrict__ target, const int* __restrict__ idx,
@@ -114,24 +149,27 @@ __global__ void __launch_bounds__(256) k_mlp_grad(const float* __restrict__ para
   const int b0 = blockIdx.x * kMlpTile;
   constexpr int TH = kMlpTile * kMlpHidden;
 
-  for (int i = t; i < kMlpParams; i += blockDim.x) P[i] = params[i];
+  for (int i = t; i < kMlpParams; i += blockDim.x) {
+    const bool bias = (i >= kMlpOffB1 && i < kMlpOffW2) || (i >= kMlpOffB2 && i < kMlpOffW3) || i == kMlpOffB3;
+    P[i] = bias ? params[i] : mlp_round<BF16>(params[i]);
+  }
   for (int i = t; i < kMlpTile * kMlpIn; i += blockDim.x) {
     const int b = i / kMlpIn, k = i % kMlpIn, s = b0 + b;
-    X[i] = s < n ? feats[static_cast<size_t>(idx ? idx[s] : s) * kMlpIn + k] : 0.0f;
+    X[i] = s < n ? mlp_round<BF16>(feats[static_cast<size_t>(idx ? idx[s] : s) * kMlpIn + k]) : 0.0f;
   }
   __syncthreads();
   for (int i = t; i < TH; i += blockDim.x) {
     const int b = i / kMlpHidden, h = i % kMlpHidden;
     float a = P[kMlpOffB1 + h];
     for (int k = 0; k < kMlpIn; ++k) a = fmaf(X[b * kMlpIn + k], P[kMlpOffW1 + k * kMlpHidden + h], a);
-    H1[i] = fmaxf(a, 0.0f);
+    H1[i] = mlp_round<BF16>(fmaxf(a, 0.0f));
   }
   __syncthreads();
   for (int i = t; i < TH; i += blockDim.x) {
     const int b = i / kMlpHidden, o = i % kMlpHidden;
     float a = P[kMlpOffB2 + o];
     for (int h = 0; h < kMlpHidden; ++h) a = fmaf(H1[b * kMlpHidden + h], P[kMlpOffW2 + h * kMlpHidden + o], a);
-    H2[i] = fmaxf(a, 0.0f);
+    H2[i] = mlp_round<BF16>(fmaxf(a, 0.0f));
   }
   __syncthreads();
   if (t < kMlpTile) {
@@ -186,13 +224,18 @@ __global__ void __launch_bounds__(256) k_mlp_grad(const float* __restrict__ para
 }
 
 int launch_mlp_grad(const float* params, const float* feats, const float* target, const int* idx, int n,
-                    float* partial, float* partial_loss, cudaStream_t st) {
+                    float* partial, float* partial_loss, cudaStream_t st, bool bf16) {
   if (n <= 0) return 0;
   const int nblk = (n + kMlpTile - 1) / kMlpTile;
   const size_t smem = mlp_grad_smem_bytes();
-  cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-  k_mlp_grad<<<nblk, 256, smem, st>>>(params, feats, target, idx, n, 1.0f / static_cast<float>(n), partial,
-                                      partial_loss);
+  const float inv_n = 1.0f / static_cast<float>(n);
+  if (bf16) {
+    cudaFuncSetAttribute(k_mlp_grad<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    k_mlp_grad<true><<<nblk, 256, smem, st>>>(params, feats, target, idx, n, inv_n, partial, partial_loss);
+  } else {
+    cudaFuncSetAttribute(k_mlp_grad<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    k_mlp_grad<false><<<nblk, 256, smem, st>>>(params, feats, target, idx, n, inv_n, partial, partial_loss);
+  }
   return nblk;
 }
 

@@ -32,14 +32,16 @@ constexpr float kSchedPredMax = 40.0f;  // log(1 + work) mapped onto the buckets
 // Features of every (item, cell): n_items * ncell rows of kMlpIn floats.
 void launch_cell_features(const BatchItem* items, int n_items, const Geom& g, float* feats, cudaStream_t st);
 
-// pred[i] = MLP(feats[i]).
-void launch_mlp_predict(const float* params, const float* feats, int n, float* pred, cudaStream_t st);
+// pred[i] = MLP(feats[i]); bf16: the BF16 forward pass (weights, inputs and
+// activations rounded to bfloat16, FP32 accumulation).
+void launch_mlp_predict(const float* params, const float* feats, int n, float* pred, cudaStream_t st,
+                        bool bf16 = false);
 
 // Mean-squared-error gradient over the n samples idx[0..n) (idx null: 0..n)
 // of (feats, target): per-CTA partial sums, reduced in a fixed order by
 // launch_mlp_reduce or launch_adam. Returns the number of CTAs used.
 int launch_mlp_grad(const float* params, const float* feats, const float* target, const int* idx, int n,
-                    float* partial, float* partial_loss, cudaStream_t st);
+                    float* partial, float* partial_loss, cudaStream_t st, bool bf16 = false);
 size_t mlp_grad_smem_bytes();
 void launch_mlp_reduce(const float* partial, const float* partial_loss, int nblk, float* grad, float* loss,
                        cudaStream_t st);

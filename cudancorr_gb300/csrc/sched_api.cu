@@ -120,6 +120,14 @@ int ncorr_sched_set_params(ncorr_sched* s, const float* in, int64_t n) {
   return NCORR_OK;
 }
 
+int ncorr_sched_set_precision(ncorr_sched* s, int precision) {
+  if (int rc = check_sched(s)) return rc;
+  if (precision != NCORR_MLP_FP32 && precision != NCORR_MLP_BF16)
+    return fail(NCORR_ERR_INVALID_ARGUMENT, "precision must be NCORR_MLP_FP32 or NCORR_MLP_BF16");
+  s->bf16 = precision == NCORR_MLP_BF16;
+  return NCORR_OK;
+}
+
 int ncorr_sched_predict(ncorr_sched* s, const float* feats, int64_t n, float* out) {
   if (int rc = check_sched(s)) return rc;
   if (n < 0 || n > (int64_t(1) << 30) || (n > 0 && (!feats || !out)))
@@ -128,7 +136,7 @@ int ncorr_sched_predict(ncorr_sched* s, const float* feats, int64_t n, float* ou
   if (int rc = upload(s, feats, nullptr, n)) return rc;
   CU(s->pred.ensure(static_cast<size_t>(n) * sizeof(float)));
   launch_mlp_predict(s->params.as<float>(), s->feats.as<float>(), static_cast<int>(n), s->pred.as<float>(),
-                     s->stream);
+                     s->stream, s->bf16);
   CU(cudaGetLastError());
   CU(cudaMemcpyAsync(out, s->pred.p, static_cast<size_t>(n) * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
   CU(cudaStreamSynchronize(s->stream));
@@ -144,7 +152,7 @@ int ncorr_sched_gradient(ncorr_sched* s, const float* feats, const float* target
   if (int rc = ensure_partials(s, n)) return rc;
   const int nblk = launch_mlp_grad(s->params.as<float>(), s->feats.as<float>(), s->target.as<float>(), nullptr,
                                    static_cast<int>(n), s->partial.as<float>(), s->partial_loss.as<float>(),
-                                   s->stream);
+                                   s->stream, s->bf16);
   launch_mlp_reduce(s->partial.as<float>(), s->partial_loss.as<float>(), nblk, s->grad.as<float>(),
                     s->loss.as<float>(), s->stream);
   CU(cudaGetLastError());
@@ -186,7 +194,7 @@ int ncorr_sched_train(ncorr_sched* s, const float* feats, const float* target, i
       const int nb = static_cast<int>(std::min<int64_t>(batch, n - b0));
       const int nblk = launch_mlp_grad(s->params.as<float>(), s->feats.as<float>(), s->target.as<float>(),
                                        s->idx.as<int>() + b0, nb, s->partial.as<float>(),
-                                       s->partial_loss.as<float>(), s->stream);
+                                       s->partial_loss.as<float>(), s->stream, s->bf16);
       launch_adam(s->params.as<float>(), s->partial.as<float>(), nblk, s->m.as<float>(), s->v.as<float>(),
                   ++s->step, lr, s->stream);
     }
@@ -196,7 +204,7 @@ int ncorr_sched_train(ncorr_sched* s, const float* feats, const float* target, i
     // Mean squared error of the trained model over all n samples.
     const int nblk = launch_mlp_grad(s->params.as<float>(), s->feats.as<float>(), s->target.as<float>(), nullptr,
                                      static_cast<int>(n), s->partial.as<float>(), s->partial_loss.as<float>(),
-                                     s->stream);
+                                     s->stream, s->bf16);
     launch_mlp_reduce(s->partial.as<float>(), s->partial_loss.as<float>(), nblk, s->grad.as<float>(),
                       s->loss.as<float>(), s->stream);
     float l = 0.0f;

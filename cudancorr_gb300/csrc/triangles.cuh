@@ -214,17 +214,17 @@ __device__ __forceinline__ void add128(unsigned long long* w, long long v) {
 //   %4-%6  the row's offset d_j, %7 rho_j^2, %8 2 rho_j, %9 the row's key
 //          (histogram base + bin_j * nb^2 * code scale)
 //   %10 table scale, %11/%12 table address bias and last entry, %13 nb * code
-//   scale, %14 -M, %15 dummy address, %16 rbit, %17 mask of the masked
-//   candidate (diagonal tiles: l < j)
-//   column c: %(18+5c)-%(20+5c) its offset scaled by -2, %(21+5c) rho_l,
-//   %(22+5c) its key (bin_l * nb * code scale)
+//   scale, %14 -M, %15 dummy address, %16 rbit, %17-%20 masks of column
+//   slots 0-3 (diagonal rows: 1 below the row's slot, l < j in it, 0 above)
+//   column c: %(21+5c)-%(23+5c) its offset scaled by -2, %(24+5c) rho_l,
+//   %(25+5c) its key (bin_l * nb * code scale)
 // One asm statement per row lets all table loads issue before the first
 // reduction; in separate statements each load would wait behind the previous
 // candidate's reduction, which may touch the same shared-memory word as far
 // as the compiler can tell.
 #define NCORR_DECL(C)                                                     \
-  ".reg .f32 pp" #C ", s" #C ", v" #C ", y" #C ", t" #C ", H" #C ";\n\t"  \
-  ".reg .b32 ia" #C ", code" #C ", key" #C ", adr" #C ";\n\t"             \
+  ".reg .f32 pp" #C ", s" #C ", v" #C ", t" #C ", H" #C ";\n\t"           \
+  ".reg .b32 y" #C ", ia" #C ", code" #C ", key" #C ", adr" #C ";\n\t"     \
   ".reg .pred ok" #C ", upd" #C ", nco" #C ", wq" #C ";\n\t"
 #define NCORR_CLS(C, LX, LY, LZ, B)                  \
   "mul.rn.f32 pp" #C ", %4, " LX ";\n\t"             \
@@ -233,8 +233,7 @@ __device__ __forceinline__ void add128(unsigned long long* w, long long v) {
   "fma.rn.f32 s" #C ", " B ", " B ", %7;\n\t"        \
   "add.rn.f32 v" #C ", pp" #C ", s" #C ";\n\t"       \
   "fma.rn.f32 y" #C ", v" #C ", %10, 0f4B000000;\n\t" \
-  "mov.b32 ia" #C ", y" #C ";\n\t"                   \
-  "add.u32 ia" #C ", ia" #C ", %11;\n\t"             \
+  "add.u32 ia" #C ", y" #C ", %11;\n\t"              \
   "min.u32 ia" #C ", ia" #C ", %12;\n\t"             \
   "ld.shared.u8 code" #C ", [ia" #C "];\n\t"
 // Column operand groups, expanded through NCORR_CLSX so that a group fills
@@ -253,26 +252,27 @@ __device__ __forceinline__ void add128(unsigned long long* w, long long v) {
   "setp.ge.and.f32 nco" #C ", t" #C ", H" #C ", ok" #C ";\n\t"     \
   "setp.eq.or.u32 wq" #C ", code" #C ", 255, nco" #C ";\n\t"       \
   "@wq" #C " or.b32 " Q ", " Q ", %16;\n\t" NCORR_KEY(C, KL)
-#define NCORR_UPD_MASKED(C, B, KL, Q)                              \
+#define NCORR_UPD_MASKED(C, B, KL, Q, M)                           \
   "abs.f32 t" #C ", pp" #C ";\n\t"                                 \
   "fma.rn.f32 H" #C ", %8, " B ", %14;\n\t"                        \
-  "setp.ne.u32 inp, %17, 0;\n\t"                                   \
+  "setp.ne.u32 inp" #C ", " M ", 0;\n\t"                           \
   "setp.lt.u32 ok" #C ", code" #C ", %13;\n\t"                     \
-  "and.pred ok" #C ", ok" #C ", inp;\n\t"                          \
+  "and.pred ok" #C ", ok" #C ", inp" #C ";\n\t"                    \
   "setp.lt.and.f32 upd" #C ", t" #C ", H" #C ", ok" #C ";\n\t"     \
   "setp.ge.and.f32 nco" #C ", t" #C ", H" #C ", ok" #C ";\n\t"     \
-  "setp.eq.and.u32 car, code" #C ", 255, inp;\n\t"                 \
-  "or.pred wq" #C ", car, nco" #C ";\n\t"                          \
+  "setp.eq.and.u32 car" #C ", code" #C ", 255, inp" #C ";\n\t"     \
+  "or.pred wq" #C ", car" #C ", nco" #C ";\n\t"                    \
   "@wq" #C " or.b32 " Q ", " Q ", %16;\n\t" NCORR_KEY(C, KL)
 #define NCORR_RED(C) "red.shared.add.u32 [adr" #C "], 1;\n\t"
-#define NCORR_C0 "%18", "%19", "%20", "%21"
-#define NCORR_C1 "%23", "%24", "%25", "%26"
-#define NCORR_C2 "%28", "%29", "%30", "%31"
-#define NCORR_C3 "%33", "%34", "%35", "%36"
+#define NCORR_C0 "%21", "%22", "%23", "%24"
+#define NCORR_C1 "%26", "%27", "%28", "%29"
+#define NCORR_C2 "%31", "%32", "%33", "%34"
+#define NCORR_C3 "%36", "%37", "%38", "%39"
 #define NCORR_ROW_OPERANDS                                                                                      \
   : "+r"(q0), "+r"(q1), "+r"(q2), "+r"(q3)                                                                     \
   : "f"(r.x), "f"(r.y), "f"(r.z), "f"(r.a), "f"(r.a2r), "r"(r.key), "f"(k.tscale), "r"(k.tab_adj),             \
-    "r"(k.tab_last), "r"(k.nb_cs), "f"(k.hm), "r"(k.dummy), "r"(rbit), "r"(in), "f"(c.l[0].x), "f"(c.l[0].y), \
+    "r"(k.tab_last), "r"(k.nb_cs), "f"(k.hm), "r"(k.dummy), "r"(rbit), "r"(m0), "r"(m1), "r"(m2), "r"(m3),     \
+    "f"(c.l[0].x), "f"(c.l[0].y), \
     "f"(c.l[0].z), "f"(c.l[0].w), "r"(c.k[0]), "f"(c.l[1].x), "f"(c.l[1].y), "f"(c.l[1].z), "f"(c.l[1].w),    \
     "r"(c.k[1]), "f"(c.l[2].x), "f"(c.l[2].y), "f"(c.l[2].z), "f"(c.l[2].w), "r"(c.k[2]), "f"(c.l[3].x),        \
     "f"(c.l[3].y), "f"(c.l[3].z), "f"(c.l[3].w), "r"(c.k[3])                                                   \
@@ -297,38 +297,25 @@ struct ColV {
 // Four full candidates (column slots 0-3).
 __device__ __forceinline__ void row_full4(const RowV& r, const ColV& c, const BodyK& k, unsigned rbit, unsigned& q0,
                                           unsigned& q1, unsigned& q2, unsigned& q3) {
-  const unsigned in = 1u;
+  const unsigned m0 = 1u, m1 = 1u, m2 = 1u, m3 = 1u;
   asm volatile("{\n\t" NCORR_DECL(0) NCORR_DECL(1) NCORR_DECL(2) NCORR_DECL(3)
                NCORR_CLSX(0, NCORR_C0) NCORR_CLSX(1, NCORR_C1) NCORR_CLSX(2, NCORR_C2) NCORR_CLSX(3, NCORR_C3)
-               NCORR_UPD(0, "%21", "%22", "%0") NCORR_UPD(1, "%26", "%27", "%1") NCORR_UPD(2, "%31", "%32", "%2")
-               NCORR_UPD(3, "%36", "%37", "%3")
+               NCORR_UPD(0, "%24", "%25", "%0") NCORR_UPD(1, "%29", "%30", "%1") NCORR_UPD(2, "%34", "%35", "%2")
+               NCORR_UPD(3, "%39", "%40", "%3")
                NCORR_RED(0) NCORR_RED(1) NCORR_RED(2) NCORR_RED(3) "}" NCORR_ROW_OPERANDS);
 }
 
-// Diagonal tiles (identical lists, pairs l < j): in row group S the column
-// slots below S are full and slot S is masked by `in` (l < j).
-template <int S>
-__device__ __forceinline__ void row_diag(const RowV& r, const ColV& c, const BodyK& k, unsigned rbit, unsigned in,
-                                         unsigned& q0, unsigned& q1, unsigned& q2, unsigned& q3) {
-  if (S == 0) {
-    asm volatile("{\n\t.reg .pred inp, car;\n\t" NCORR_DECL(0) NCORR_CLSX(0, NCORR_C0)
-                 NCORR_UPD_MASKED(0, "%21", "%22", "%0") NCORR_RED(0) "}" NCORR_ROW_OPERANDS);
-  } else if (S == 1) {
-    asm volatile("{\n\t.reg .pred inp, car;\n\t" NCORR_DECL(0) NCORR_DECL(1) NCORR_CLSX(0, NCORR_C0)
-                 NCORR_CLSX(1, NCORR_C1) NCORR_UPD(0, "%21", "%22", "%0") NCORR_UPD_MASKED(1, "%26", "%27", "%1")
-                 NCORR_RED(0) NCORR_RED(1) "}" NCORR_ROW_OPERANDS);
-  } else if (S == 2) {
-    asm volatile("{\n\t.reg .pred inp, car;\n\t" NCORR_DECL(0) NCORR_DECL(1) NCORR_DECL(2) NCORR_CLSX(0, NCORR_C0)
-                 NCORR_CLSX(1, NCORR_C1) NCORR_CLSX(2, NCORR_C2) NCORR_UPD(0, "%21", "%22", "%0")
-                 NCORR_UPD(1, "%26", "%27", "%1") NCORR_UPD_MASKED(2, "%31", "%32", "%2")
-                 NCORR_RED(0) NCORR_RED(1) NCORR_RED(2) "}" NCORR_ROW_OPERANDS);
-  } else {
-    asm volatile("{\n\t.reg .pred inp, car;\n\t" NCORR_DECL(0) NCORR_DECL(1) NCORR_DECL(2) NCORR_DECL(3)
-                 NCORR_CLSX(0, NCORR_C0) NCORR_CLSX(1, NCORR_C1) NCORR_CLSX(2, NCORR_C2) NCORR_CLSX(3, NCORR_C3)
-                 NCORR_UPD(0, "%21", "%22", "%0") NCORR_UPD(1, "%26", "%27", "%1") NCORR_UPD(2, "%31", "%32", "%2")
-                 NCORR_UPD_MASKED(3, "%36", "%37", "%3")
-                 NCORR_RED(0) NCORR_RED(1) NCORR_RED(2) NCORR_RED(3) "}" NCORR_ROW_OPERANDS);
-  }
+// Four candidates with a mask each (diagonal rows of identical lists, pairs
+// l < j): masked-out candidates neither count nor flag.
+__device__ __forceinline__ void row_mask4(const RowV& r, const ColV& c, const BodyK& k, unsigned rbit, unsigned m0,
+                                          unsigned m1, unsigned m2, unsigned m3, unsigned& q0, unsigned& q1,
+                                          unsigned& q2, unsigned& q3) {
+  asm volatile("{\n\t.reg .pred inp0, inp1, inp2, inp3, car0, car1, car2, car3;\n\t"
+               NCORR_DECL(0) NCORR_DECL(1) NCORR_DECL(2) NCORR_DECL(3)
+               NCORR_CLSX(0, NCORR_C0) NCORR_CLSX(1, NCORR_C1) NCORR_CLSX(2, NCORR_C2) NCORR_CLSX(3, NCORR_C3)
+               NCORR_UPD_MASKED(0, "%24", "%25", "%0", "%17") NCORR_UPD_MASKED(1, "%29", "%30", "%1", "%18")
+               NCORR_UPD_MASKED(2, "%34", "%35", "%2", "%19") NCORR_UPD_MASKED(3, "%39", "%40", "%3", "%20")
+               NCORR_RED(0) NCORR_RED(1) NCORR_RED(2) NCORR_RED(3) "}" NCORR_ROW_OPERANDS);
 }
 
 // The weighted twin of one candidate: the same classification, then the
@@ -357,8 +344,7 @@ __device__ __forceinline__ void cand_wsum(const RowV& r, const float4& l, unsign
                "fma.rn.f32 s0, %9, %9, %4;\n\t"                                                              \
                "add.rn.f32 v0, pp0, s0;\n\t"                                                                 \
                "fma.rn.f32 y0, v0, %13, 0f4B000000;\n\t"                                                     \
-               "mov.b32 ia0, y0;\n\t"                                                                        \
-               "add.u32 ia0, ia0, %14;\n\t"                                                                  \
+               "add.u32 ia0, y0, %14;\n\t"                                                                   \
                "min.u32 ia0, ia0, %15;\n\t"                                                                  \
                "ld.shared.u8 code0, [ia0];\n\t" UPD                                                          \
                "mul.rn.f32 wp, %19, %20;\n\t"                                                                \
@@ -1069,16 +1055,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_triangles(KArgs a) {
         r.key = HG ? (m & 0xffu) * kj_mul : (m & 0xffu) * kj_mul + hist_sh;
         return r;
       };
-      // Weighted and global-histogram rows: one candidate at a time; in
-      // diagonal rows slot MS is masked by `in` and the slots above it skipped.
-      auto row_slow = [&](const RowV& r, float wj, unsigned rbit, unsigned in, auto ms_tag, unsigned& q0,
+      // Weighted and global-histogram rows: one candidate at a time, each
+      // with its mask (diagonal rows; 1 elsewhere).
+      auto row_slow = [&](const RowV& r, float wj, unsigned rbit, const unsigned (&m)[kReg], unsigned& q0,
                           unsigned& q1, unsigned& q2, unsigned& q3) {
-        constexpr int MS = decltype(ms_tag)::value;
         auto one = [&](auto s_tag, unsigned& q) {
           constexpr int S = decltype(s_tag)::value;
-          if (MS >= 0 && S > MS) return;
-          constexpr bool MASK = (S == MS);
-          const unsigned ins = MASK ? in : 1u;
+          const unsigned ins = m[S];
           if (HG) {
             unsigned code;
             bool clean;
@@ -1089,7 +1072,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_triangles(KArgs a) {
               hist_add<WEIGHTED, true>(hist_s, c.hist, r.key + col.k[S] + code, (wa * wj * wsc) * wl[S]);
             if (careful) q |= rbit;
           } else if (WEIGHTED) {
-            cand_wsum<MASK>(r, col.l[S], col.k[S], ins, bk, wa * wj * wsc, wl[S], rbit, q);
+            cand_wsum<true>(r, col.l[S], col.k[S], ins, bk, wa * wj * wsc, wl[S], rbit, q);
           }
         };
         one(std::integral_constant<int, 0>(), q0);
@@ -1097,13 +1080,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_triangles(KArgs a) {
         one(std::integral_constant<int, 2>(), q2);
         one(std::integral_constant<int, 3>(), q3);
       };
-      // Rows [jb, je) of one flag group, all of one kind: MS = -1 full rows;
-      // MS = 0..3 diagonal rows (SYM: rows of the column tile itself, whose
-      // slot MS = (j - lb) / 32 is masked by l < j and slots above it empty).
-      auto rows = [&](int jb, int je, auto ms_tag, unsigned& q0, unsigned& q1, unsigned& q2, unsigned& q3) {
-        constexpr int MS = decltype(ms_tag)::value;
+      // Rows [jb, je) of one flag group, all of one kind: full rows, or
+      // diagonal rows (SYM: rows of the column tile itself, whose slot
+      // S = (j - lb) / 32 is masked by l < j and the slots above it empty).
+      auto rows = [&](int jb, int je, auto diag_tag, unsigned& q0, unsigned& q1, unsigned& q2, unsigned& q3) {
+        constexpr bool DIAG = decltype(diag_tag)::value;
+        const int S = (jb - lb) >> 5;  // diagonal rows: the row's own slot (uniform in the group)
         float4 en = l2.e[jb];
         unsigned mn = l2.m[jb];
+#pragma unroll 1
         for (int j = jb; j < je; ++j) {
           const float4 e = en;
           const unsigned m = mn;
@@ -1112,33 +1097,33 @@ __global__ void __launch_bounds__(kThreads, 1) k_triangles(KArgs a) {
           mn = l2.m[jn];
           const RowV r = make_row(e, m);
           const unsigned rbit = 1u << (j - jb);
-          const unsigned in = MS >= 0 ? (((j - lb) & 31) > lane ? 1u : 0u) : 1u;
+          unsigned mk[kReg] = {1u, 1u, 1u, 1u};
+          if (DIAG) {
+            const unsigned in = ((j - lb) & 31) > lane ? 1u : 0u;
+#pragma unroll
+            for (int s = 0; s < kReg; ++s) mk[s] = s < S ? 1u : (s == S ? in : 0u);
+          }
           if (WEIGHTED || HG) {
             const float wj = WEIGHTED ? l2.w[j] : 0.0f;
-            row_slow(r, wj, rbit, in, ms_tag, q0, q1, q2, q3);
-          } else if (MS < 0) {
+            row_slow(r, wj, rbit, mk, q0, q1, q2, q3);
+          } else if (!DIAG) {
             row_full4(r, col, bk, rbit, q0, q1, q2, q3);
           } else {
-            row_diag<(MS < 0 ? 0 : MS)>(r, col, bk, rbit, in, q0, q1, q2, q3);
+            row_mask4(r, col, bk, rbit, mk[0], mk[1], mk[2], mk[3], q0, q1, q2, q3);
           }
         }
       };
       // Groups of `group` rows (8, 16 or 32, so a group never straddles a
       // 32-row slot boundary of the diagonal); after each, the flagged
       // candidates are queued.
+#pragma unroll 1
       for (int jb = jfirst; jb < k2; jb += group) {
         const int je = min(jb + group, k2);
         unsigned q0 = 0, q1 = 0, q2 = 0, q3 = 0;
-        if (!SYM || jb >= lb + kTile) {
-          rows(jb, je, std::integral_constant<int, -1>(), q0, q1, q2, q3);
-        } else {
-          switch ((jb - lb) >> 5) {
-            case 0: rows(jb, je, std::integral_constant<int, 0>(), q0, q1, q2, q3); break;
-            case 1: rows(jb, je, std::integral_constant<int, 1>(), q0, q1, q2, q3); break;
-            case 2: rows(jb, je, std::integral_constant<int, 2>(), q0, q1, q2, q3); break;
-            default: rows(jb, je, std::integral_constant<int, 3>(), q0, q1, q2, q3); break;
-          }
-        }
+        if (!SYM || jb >= lb + kTile)
+          rows(jb, je, std::false_type(), q0, q1, q2, q3);
+        else
+          rows(jb, je, std::true_type(), q0, q1, q2, q3);
         if (__any_sync(FULL, (q0 | q1 | q2 | q3) != 0))
           cold_enqueue<SURVEY, WEIGHTED, HG>(c, jb, lb, q0, q1, q2, q3);
       }

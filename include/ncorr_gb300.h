@@ -258,6 +258,15 @@ int ncorr_sched_num_params(void);
 /* Parameter vector: W1 [28][64], b1 [64], W2 [64][64], b2 [64], w3 [64], b3. */
 int ncorr_sched_get_params(const ncorr_sched* s, float* out, int64_t cap);
 int ncorr_sched_set_params(ncorr_sched* s, const float* in, int64_t n);
+/* Arithmetic of the model's forward pass, in prediction (ncorr_sched_predict
+ * and the learned queue) and in training: NCORR_MLP_FP32 (default) or
+ * NCORR_MLP_BF16, where weights, inputs and hidden activations are rounded to
+ * bfloat16 and products are accumulated in FP32 (the master parameters, the
+ * backward pass and Adam stay FP32). No counterpart in the reference, which
+ * has no learned part. */
+enum { NCORR_MLP_FP32 = 0, NCORR_MLP_BF16 = 1 };
+int ncorr_sched_set_precision(ncorr_sched* s, int precision);
+
 /* out[i] = model(feats[i]) for n host rows of 28 floats. */
 int ncorr_sched_predict(ncorr_sched* s, const float* feats, int64_t n, float* out);
 /* Gradient of the mean squared error (1/n) sum (model(x_i) - t_i)^2 over n

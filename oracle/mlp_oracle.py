@@ -33,25 +33,42 @@ def unpack(p):
     return w1, b1, w2, b2, w3, b3
 
 
-def forward(p, x):
-    """Predictions for the rows of x (n x 28)."""
+def bf16(a):
+    """Round float32 values to bfloat16 (nearest, ties to even), as float64."""
+    b = np.ascontiguousarray(np.asarray(a, dtype=np.float32)).view(np.uint32).astype(np.uint64)
+    b = (b + 0x7FFF + ((b >> 16) & 1)) & 0xFFFF0000
+    return b.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def forward(p, x, bf16_forward=False):
+    """Predictions for the rows of x (n x 28). bf16_forward: the BF16 forward
+    pass of the engine's kernels -- weights, inputs and hidden activations
+    rounded to bfloat16, biases not, sums in (here) float64."""
     w1, b1, w2, b2, w3, b3 = unpack(p)
     x = np.asarray(x, dtype=np.float64)
-    h1 = np.maximum(x @ w1 + b1, 0.0)
-    h2 = np.maximum(h1 @ w2 + b2, 0.0)
+    r = bf16 if bf16_forward else (lambda a: np.asarray(a, dtype=np.float64))
+    if bf16_forward:
+        w1, w2, w3 = r(w1), r(w2), r(w3)
+    h1 = r(np.maximum(r(x) @ w1 + b1, 0.0))
+    h2 = r(np.maximum(h1 @ w2 + b2, 0.0))
     return h2 @ w3 + b3
 
 
-def loss_and_grad(p, x, t):
-    """(sum of squared errors, gradient of the mean squared error)."""
+def loss_and_grad(p, x, t, bf16_forward=False):
+    """(sum of squared errors, gradient of the mean squared error).
+    bf16_forward: the forward pass rounds weights, inputs and activations to
+    bfloat16 and the backward pass uses the rounded values."""
     w1, b1, w2, b2, w3, b3 = unpack(p)
     x = np.asarray(x, dtype=np.float64)
     t = np.asarray(t, dtype=np.float64)
+    r = bf16 if bf16_forward else (lambda a: a)
+    if bf16_forward:
+        w1, w2, w3, x = r(w1), r(w2), r(w3), r(x)
     n = x.shape[0]
     z1 = x @ w1 + b1
-    h1 = np.maximum(z1, 0.0)
+    h1 = r(np.maximum(z1, 0.0))
     z2 = h1 @ w2 + b2
-    h2 = np.maximum(z2, 0.0)
+    h2 = r(np.maximum(z2, 0.0))
     y = h2 @ w3 + b3
     r = y - t
     dy = 2.0 * r / n
