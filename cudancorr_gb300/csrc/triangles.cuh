@@ -318,6 +318,17 @@ __device__ __forceinline__ void row_mask4(const RowV& r, const ColV& c, const Bo
                NCORR_RED(0) NCORR_RED(1) NCORR_RED(2) NCORR_RED(3) "}" NCORR_ROW_OPERANDS);
 }
 
+// Two candidates with masks (column slots 0-1; diagonal rows of the first two
+// 32-row groups of a tile, where slots 2-3 hold no pair).
+__device__ __forceinline__ void row_mask2(const RowV& r, const ColV& c, const BodyK& k, unsigned rbit, unsigned m0,
+                                          unsigned m1, unsigned& q0, unsigned& q1, unsigned& q2, unsigned& q3) {
+  const unsigned m2 = 0u, m3 = 0u;
+  asm volatile("{\n\t.reg .pred inp0, inp1, car0, car1;\n\t" NCORR_DECL(0) NCORR_DECL(1)
+               NCORR_CLSX(0, NCORR_C0) NCORR_CLSX(1, NCORR_C1)
+               NCORR_UPD_MASKED(0, "%24", "%25", "%0", "%17") NCORR_UPD_MASKED(1, "%29", "%30", "%1", "%18")
+               NCORR_RED(0) NCORR_RED(1) "}" NCORR_ROW_OPERANDS);
+}
+
 // The weighted twin of one candidate: the same classification, then the
 // fixed-point weight w_row * w_l (|value| <= 2^30 by the choice of the scale,
 // so the 32-bit conversion is exact and equals the 64-bit one) added into the
@@ -1088,7 +1099,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_triangles(KArgs a) {
         const int S = (jb - lb) >> 5;  // diagonal rows: the row's own slot (uniform in the group)
         float4 en = l2.e[jb];
         unsigned mn = l2.m[jb];
-#pragma unroll 1
+#pragma unroll(DIAG ? 1 : 2)
         for (int j = jb; j < je; ++j) {
           const float4 e = en;
           const unsigned m = mn;
@@ -1108,6 +1119,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_triangles(KArgs a) {
             row_slow(r, wj, rbit, mk, q0, q1, q2, q3);
           } else if (!DIAG) {
             row_full4(r, col, bk, rbit, q0, q1, q2, q3);
+          } else if (S < 2) {
+            row_mask2(r, col, bk, rbit, mk[0], mk[1], q0, q1, q2, q3);
           } else {
             row_mask4(r, col, bk, rbit, mk[0], mk[1], mk[2], mk[3], q0, q1, q2, q3);
           }

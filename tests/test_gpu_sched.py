@@ -144,3 +144,61 @@ def test_model_learns_cell_work(engine_lib):
     var = np.var(yt)
     # The float64 oracle trained the same way reaches about 0.31 of the variance.
     assert mse < 0.5 * var, (mse, var)
+
+
+def test_bf16_forward_matches_cpu_oracle(engine_lib):
+    """The BF16 forward pass (weights, inputs and hidden activations rounded
+    to bfloat16, FP32 accumulation) against the oracle's restatement of the
+    same roundings with float64 sums. Tolerance: the two sum the same
+    products in different precision, so a sum that falls next to a bfloat16
+    rounding boundary can round one bfloat16 step differently; 99% of the
+    outputs agree to 1e-4 of the output scale, all to 2e-2. Against the FP32
+    model the BF16 outputs stay within 0.1 of the scale."""
+    rng = np.random.default_rng(21)
+    model = api.WorkModel(seed=8)
+    p = model.get_params().astype(np.float64)
+    x = rng.uniform(0.0, 7.0, (1000, 28)).astype(np.float32)
+    y32 = model.predict(x)
+    model.set_precision(api.MLP_BF16)
+    y16 = model.predict(x)
+    y_o = M.forward(p, x, bf16_forward=True)
+    scale = max(1.0, float(np.max(np.abs(y_o))))
+    err = np.abs(y16 - y_o)
+    assert np.quantile(err, 0.99) <= 1e-4 * scale
+    assert err.max() <= 2e-2 * scale
+    assert np.max(np.abs(y16 - y32)) <= 0.1 * scale
+    assert np.max(np.abs(y16 - y32)) > 0  # the roundings do happen
+    # Training gradient with the BF16 forward pass.
+    t = rng.uniform(5.0, 20.0, 300).astype(np.float32)
+    g, sse = model.gradient(x[:300], t)
+    sse_o, g_o = M.loss_and_grad(p, x[:300].astype(np.float64), t.astype(np.float64), bf16_forward=True)
+    assert abs(sse - sse_o) <= 1e-3 * sse_o
+    assert np.max(np.abs(g - g_o)) <= 1e-2 * np.max(np.abs(g_o))
+    assert np.mean(np.abs(g - g_o)) <= 1e-3 * np.max(np.abs(g_o))
+    model.close()
+
+
+def test_bf16_model_orders_like_fp32_and_keeps_counts():
+    """A work model trained with the BF16 forward pass predicts cell work like
+    the FP32 one on a held-out catalogue, and the learned queue it builds
+    gives counts identical to the dynamic schedule (the order never changes
+    the counts)."""
+    x, y = training_rows([61, 62, 63])
+    m32 = api.WorkModel(seed=3)
+    m32.train(x, y, epochs=60, batch=256, lr=3e-3, seed=4)
+    m16 = api.WorkModel(seed=3)
+    m16.set_precision(api.MLP_BF16)
+    m16.train(x, y, epochs=60, batch=256, lr=3e-3, seed=4)
+    p, box, edges = small_sp(64)
+    h_dyn, _, feats, work = counts(box, edges, p, record=True)
+    keep = feats[:, 0] > 0
+    yt = np.log1p(work[keep])
+    p32 = m32.predict(feats[keep]).astype(np.float64)
+    p16 = m16.predict(feats[keep]).astype(np.float64)
+    r2_32 = 1.0 - np.mean((p32 - yt) ** 2) / np.var(yt)
+    r2_16 = 1.0 - np.mean((p16 - yt) ** 2) / np.var(yt)
+    assert r2_16 > 0.3 and r2_16 > r2_32 - 0.1
+    h16, _ = counts(box, edges, p, mode=api.SCHED_LEARNED, model=m16)
+    assert np.array_equal(h16, h_dyn)
+    m32.close()
+    m16.close()
