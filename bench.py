@@ -427,7 +427,8 @@ def north_star_block() -> dict:
         if ref_counts is None:
             ref_counts = h
         same = same and bool(np.array_equal(h, ref_counts))
-        sched[name] = {"call_ms": ms, "kernel_ms": st["ms_count"], "triangles": int(st["triangles"])}
+        sched[name] = {"call_ms": ms, "kernel_ms": st["ms_count"], "triangles": int(st["triangles"]),
+                       "tail_idle": st["tail_idle"]}
     corr.close()
     keep = f[:, 0] > 0
     y = np.log1p(w[keep])

@@ -73,6 +73,7 @@ class NcorrStats(ctypes.Structure):
         ("triangles", ctypes.c_uint64), ("n_flagged_rows", ctypes.c_uint64), ("n_queued", ctypes.c_uint64),
         ("weighted", ctypes.c_int), ("symmetric", ctypes.c_int),
         ("grid_ctas", ctypes.c_int), ("list_capacity", ctypes.c_int), ("overflow", ctypes.c_double),
+        ("tail_idle", ctypes.c_double),
     ]
 
     def as_dict(self) -> dict:

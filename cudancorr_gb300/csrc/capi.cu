@@ -140,6 +140,7 @@ int run(ncorr_handle* h, const double4_16a* d1, int n1, const double4_16a* d2, i
   if (weighted) CU(h->slab_w.ensure(slab_n * sizeof(float)));
   CU(h->slab_q.ensure(static_cast<size_t>(shp.grid) * kWarps * kQueueCap * sizeof(unsigned long long)));
   CU(h->slab_x.ensure(static_cast<size_t>(shp.grid) * kWarps * 32 * sizeof(ExactEntry)));
+  CU(h->cta_time.ensure(static_cast<size_t>(shp.grid) * 2 * sizeof(unsigned long long)));
 
   const size_t hist_words = weighted ? 2 * static_cast<size_t>(nbin) : static_cast<size_t>(nbin);
   CU(h->d_hist.ensure(hist_words * sizeof(unsigned long long)));
@@ -209,6 +210,7 @@ int run(ncorr_handle* h, const double4_16a* d1, int n1, const double4_16a* d2, i
   a.slab_x = h->slab_x.as<ExactEntry>();
   a.kcap2 = shp.kcap2;
   a.kcap3 = shp.kcap3;
+  a.cta_time = h->cta_time.as<unsigned long long>();
   a.code_scale = code_scale;
   a.wscale = wscale;
   a.stats = h->d_stats.as<unsigned long long>();
@@ -244,6 +246,10 @@ int run(ncorr_handle* h, const double4_16a* d1, int n1, const double4_16a* d2, i
   unsigned long long st_host[8];
   unsigned long long total = 0;
   int kflags = 0;
+  std::vector<unsigned long long> cta_t(static_cast<size_t>(shp.grid) * 2, 0ull);
+  if (n1 > 0)
+    CU(cudaMemcpyAsync(cta_t.data(), h->cta_time.p, cta_t.size() * sizeof(unsigned long long),
+                       cudaMemcpyDeviceToHost, st));
   CU(cudaMemcpyAsync(h->counts_all.data(), h->d_out.p, nbin * sizeof(double), cudaMemcpyDeviceToHost, st));
   CU(cudaMemcpyAsync(st_host, h->d_stats.p, sizeof(st_host), cudaMemcpyDeviceToHost, st));
   CU(cudaMemcpyAsync(&total, h->d_total.p, sizeof(total), cudaMemcpyDeviceToHost, st));
@@ -278,6 +284,7 @@ int run(ncorr_handle* h, const double4_16a* d1, int n1, const double4_16a* d2, i
   s.symmetric = sym6 ? 6 : (sym ? 2 : 1);
   s.grid_ctas = shp.grid;
   s.list_capacity = shp.kcap2;
+  s.tail_idle = n1 > 0 ? tail_idle_fraction(cta_t, shp.grid) : 0.0;
   return NCORR_OK;
 }
 
@@ -449,7 +456,7 @@ void ncorr_destroy(ncorr_handle* h) {
   }
   for (DevBuf* b : {&h->d_table, &h->d_flags, &h->d_wmax, &h->d_work, &h->d_bound, &h->d_hist,
                     &h->d_out, &h->d_stats, &h->d_total, &h->slab_e, &h->slab_m, &h->slab_p,
-                    &h->slab_w, &h->slab_q, &h->slab_x, &h->xq, &h->xq_count, &h->d_args, &h->d_items, &h->d_cell_work,
+                    &h->slab_w, &h->slab_q, &h->slab_x, &h->cta_time, &h->xq, &h->xq_count, &h->d_args, &h->d_items, &h->d_cell_work,
                     &h->d_feats, &h->q_item, &h->q_anchor, &h->rp_pos, &h->rp_ab, &h->rp_rel, &h->rp_meta})
     b->release();
   h->order.release();

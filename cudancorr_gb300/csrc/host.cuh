@@ -142,7 +142,7 @@ struct ncorr_handle {
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   ncorr_host::CatDev cat[3];
   ncorr_host::DevBuf d_table, d_flags, d_wmax, d_work, d_bound, d_hist, d_out, d_stats, d_total;
-  ncorr_host::DevBuf slab_e, slab_m, slab_p, slab_w, slab_q, slab_x;
+  ncorr_host::DevBuf slab_e, slab_m, slab_p, slab_w, slab_q, slab_x, cta_time;
   ncorr_host::DevBuf xq, xq_count;  // deferred exact candidates
   ncorr_host::DevBuf d_args;        // global copy of the triangle kernel's arguments
   unsigned xq_cap = 0;
@@ -305,6 +305,22 @@ inline bool tri_shape(int nb, bool survey, bool sym, bool weighted, bool hg, int
   out->kcap2 = ((std::max(bound2, 1) + 31) / 32) * 32;
   out->kcap3 = sym ? 0 : ((std::max(bound3, 1) + 31) / 32) * 32;
   return true;
+}
+
+// Share of the launch's CTA-time spent idle at its end: CTA b ran from
+// t[2b] to t[2b+1] (ns); the launch lasted from the first start to the last
+// end.
+inline double tail_idle_fraction(const std::vector<unsigned long long>& t, int grid) {
+  if (grid <= 0) return 0.0;
+  unsigned long long t0 = ~0ull, t1 = 0;
+  for (int b = 0; b < grid; ++b) {
+    t0 = std::min(t0, t[2 * b]);
+    t1 = std::max(t1, t[2 * b + 1]);
+  }
+  if (t1 <= t0) return 0.0;
+  double idle = 0.0;
+  for (int b = 0; b < grid; ++b) idle += static_cast<double>(t1 - t[2 * b + 1]);
+  return idle / (static_cast<double>(grid) * static_cast<double>(t1 - t0));
 }
 
 // Entries of the per-warp list slabs of a launch.

@@ -131,6 +131,9 @@ struct KArgs {
   // (4: u32 counts, 8: int64 sums, 1: global histogram, bins unscaled).
   int code_scale;
   unsigned long long* stats;  // exact tris, exact pairs, anchors, W, P, flagged rows, queued
+  // Optional: per CTA, its start and end time (globaltimer, ns), from which
+  // the host measures how long CTAs sat idle at the end of the launch.
+  unsigned long long* cta_time;
   // Deferred exact candidates (null: settle them in place).
   ExactEntry* xq;
   unsigned* xq_count;
@@ -681,6 +684,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_triangles(KArgs a) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const unsigned FULL = 0xffffffffu;
   const unsigned lt_mask = (1u << lane) - 1u;
+  if (a.cta_time && tid == 0) {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    a.cta_time[2 * blockIdx.x] = t;
+  }
   const SmemLayout L = make_layout(nb, WEIGHTED, HG, a.hist_copies);
   unsigned char* tab = smem + L.table;
   unsigned char* hist_s = smem + L.hist;
@@ -1147,6 +1155,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_triangles(KArgs a) {
   if (lane == 0 && held) atomicAdd(&s_slot, ~0ull);
   cold_flush_exact<SURVEY, WEIGHTED>(c);
   __syncthreads();
+  if (a.cta_time && tid == 0) {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    a.cta_time[2 * blockIdx.x + 1] = t;
+  }
   if (!HG) {
     // Every warp has left: drain what the CTA histogram holds.
     const unsigned owner = static_cast<unsigned>(s_slot >> 32);

@@ -69,6 +69,8 @@ typedef struct ncorr_stats {
   double overflow;         /* rppi: count (or weight) of triangles whose reference index lies
                               past triCountsAll_ (pi bin numMinorBins from FP32 rounding);
                               the reference writes those out of bounds */
+  double tail_idle;        /* threeD: share of the triangle kernel's CTA-time spent idle while
+                              the last CTAs finished (0: all CTAs ended together) */
 } ncorr_stats;
 
 /* ncorr::ncorr(double3 box, int bin_type, std::vector<double>& bins,
