@@ -243,7 +243,7 @@ int plan(ncorr_batch* b, int autotune) {
     if (h->g.nc[d] < 4 || __builtin_fma(-static_cast<double>(h->g.nc[d]), h->g.cell, h->box[d]) != 0.0)
       divisible = false;
   const int elem = b->weighted ? 8 : 4;
-  b->hg = static_cast<long>(nbin) * elem > kHistSmemMax || nb * elem > 0xFD;
+  b->hg = hist_global(nb, elem);
   const int code_scale = b->hg ? 1 : elem;
   {
     std::vector<unsigned char> tab;
@@ -320,7 +320,8 @@ int plan(ncorr_batch* b, int autotune) {
   }
   if (cands.empty()) {
     Cand c{h->sub_j, 1, TriShape()};
-    if (!shape(b, 1, kmax, &c.shp)) return fail(NCORR_ERR_CUDA, "triangle kernel does not fit on the device");
+    if (!shape(b, 1, kmax, &c.shp)) return fail(NCORR_ERR_CUDA, "triangle kernel does not fit on the device, or a 27-cell neighbourhood holds "
+                                  "more than 2^24 points");
     cands.push_back(c);
   }
   size_t slab_n = 0;
@@ -422,7 +423,8 @@ int plan(ncorr_batch* b, int autotune) {
   // The launch that the graph records sets no attribute: the occupancy query
   // sets the kernel's shared-memory limit to the chosen size.
   if (triangles_occupancy(h->survey != 0, b->sym, b->weighted, b->hg, b->smem) <= 0)
-    return fail(NCORR_ERR_CUDA, "triangle kernel does not fit on the device");
+    return fail(NCORR_ERR_CUDA, "triangle kernel does not fit on the device, or a 27-cell neighbourhood holds "
+                                  "more than 2^24 points");
   CU(cudaStreamSynchronize(s));
   b->st.ms_autotune = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 

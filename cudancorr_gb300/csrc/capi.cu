@@ -113,10 +113,10 @@ int run(ncorr_handle* h, const double4_16a* d1, int n1, const double4_16a* d2, i
         sym6 = false;
 
   // CTA histogram in shared memory when it fits; a bin's byte stride is
-  // encoded in the table codes (u8, so at most 0xFD).
+  // encoded in the table codes (u8).
   const int nbin = h->nb * h->nb * h->nb;
   const int elem = weighted ? 8 : 4;
-  bool hg = static_cast<long>(nbin) * elem > kHistSmemMax || h->nb * elem > 0xFD;
+  const bool hg = hist_global(h->nb, elem);
   const int code_scale = hg ? 1 : elem;
   if (h->table_scale != code_scale) {
     build_table(h->g, code_scale, h->table);
@@ -132,7 +132,8 @@ int run(ncorr_handle* h, const double4_16a* d1, int n1, const double4_16a* d2, i
   CU(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->device));
   TriShape shp;
   if (!tri_shape(h->nb, h->survey != 0, sym, weighted, hg, h->hist_copies, nsm, n1, bound[0], bound[1], &shp))
-    return fail(NCORR_ERR_CUDA, "triangle kernel does not fit on the device");
+    return fail(NCORR_ERR_CUDA, "triangle kernel does not fit on the device, or a 27-cell neighbourhood holds "
+                                "more than 2^24 points");
   const size_t slab_n = tri_slab_entries(shp);
   CU(h->slab_e.ensure(slab_n * sizeof(float4)));
   CU(h->slab_m.ensure(slab_n * sizeof(unsigned)));
@@ -996,7 +997,7 @@ static int count_noalloc_impl(const double box[3], const double* edges, int n_ed
   }
   const int nbin = g.nb * g.nb * g.nb;
   const int elem = weighted ? 8 : 4;
-  const bool hg = static_cast<long>(nbin) * elem > kHistSmemMax || g.nb * elem > 0xFD;
+  const bool hg = hist_global(g.nb, elem);
   const int code_scale = hg ? 1 : elem;
   // Launch shape; the grid shrinks until the per-warp slabs (lists sized by
   // the largest 27-cell occupancy, careful queues, exact buffers) fit the
@@ -1005,7 +1006,8 @@ static int count_noalloc_impl(const double box[3], const double* edges, int n_ed
   CU(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   TriShape shp;
   if (!tri_shape(g.nb, g.survey != 0, sym, weighted, hg, 1, nsm, n1, hbound[0], hbound[1], &shp))
-    return fail(NCORR_ERR_CUDA, "triangle kernel does not fit on the device");
+    return fail(NCORR_ERR_CUDA, "triangle kernel does not fit on the device, or a 27-cell neighbourhood holds "
+                                "more than 2^24 points");
   const size_t per_warp_entries = static_cast<size_t>(shp.kcap2) + shp.kcap3;
   const size_t per_cta = kWarps * (per_warp_entries * (sizeof(float4) + sizeof(unsigned) + sizeof(int) +
                                                        sizeof(float)) +

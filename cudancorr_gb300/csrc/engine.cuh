@@ -30,6 +30,22 @@ constexpr int kTableSize = NCORR_TABLE_SIZE;  // bin table entries (u8)
 constexpr unsigned kCodeReject = 0xFEu;
 constexpr unsigned kCodeCareful = 0xFFu;
 
+// The CTA histogram of the triangle kernel holds, for every (bin_j, bin_l),
+// a row of nb + 2 bins: the nb real ones, then two sinks that rejected and
+// careful candidates add into (the bin table's codes for them), so the
+// candidate bodies need not test the code. Nothing reads the sinks.
+__host__ __device__ inline int hist_row(int nb) { return nb + 2; }
+__host__ __device__ inline int hist_words(int nb) { return nb * nb * hist_row(nb); }
+// Bin-table codes of "reject" and "careful": with a CTA histogram (code
+// scale = the byte stride of a bin, > 1) the two sink bins of the row; with
+// the global histogram (code scale 1) the plain markers above.
+__host__ __device__ inline unsigned table_code_reject(int nb, int cs) {
+  return cs > 1 ? static_cast<unsigned>(nb * cs) : kCodeReject;
+}
+__host__ __device__ inline unsigned table_code_careful(int nb, int cs) {
+  return cs > 1 ? static_cast<unsigned>((nb + 1) * cs) : kCodeCareful;
+}
+
 // Error flags written by kernels.
 constexpr int kFlagOutOfGrid = 1;     // a point the reference would index out of bounds
 constexpr int kFlagNonFinite = 2;

@@ -57,6 +57,16 @@ constexpr int kDefaultDotPattern = 2;
 // memory; what the kernel leaves of the SM's 256 KB serves as L1 for the
 // neighbour lists.
 constexpr long kHistSmemMax = 96 * 1024;
+
+// Whether the triangle kernel keeps its histogram in global memory: the CTA
+// histogram (nb^2 (nb + 2) bins of elem bytes, sinks included) must fit
+// kHistSmemMax and its table codes, the careful sink's included, one byte.
+// Largest neighbour list (points of one 27-cell neighbourhood) per anchor.
+constexpr int kListMax = 1 << 24;
+
+inline bool hist_global(int nb, int elem) {
+  return static_cast<long>(hist_words(nb)) * elem > kHistSmemMax || (nb + 1) * elem > 0xFF;
+}
 constexpr unsigned kExactQueueCap = 1u << 24;  // 16M entries, 256 MiB
 
 struct DevBuf {
@@ -238,9 +248,10 @@ inline void set_error_model(Geom& g) {
 
 // Bin table: entry i covers every v with rint(v * scale) == i. Its code is the
 // bin that contains the whole error band of every such v (times code_scale,
-// the byte stride of a bin in the CTA histogram), kCodeReject when the band
-// lies outside (rmin^2, rmax^2), or kCodeCareful otherwise.
-// `tab` holds kTableSize entries.
+// the byte stride of a bin in the CTA histogram), "reject" when the band lies
+// outside (rmin^2, rmax^2), or "careful" otherwise (table_code_reject /
+// table_code_careful: sink bins of the CTA histogram, or plain markers for
+// the global one). `tab` holds kTableSize entries.
 inline void build_table(Geom& g, int code_scale, unsigned char* tab) {
   const int n = kTableSize;
   const double vmax = g.sqr_rmax * 1.05;
@@ -248,6 +259,8 @@ inline void build_table(Geom& g, int code_scale, unsigned char* tab) {
   g.tab_scale = scale;
   g.tab_n = n;
   const double ka = g.ka, kb = g.kb;
+  const auto rej = static_cast<unsigned char>(table_code_reject(g.nb, code_scale));
+  const auto car = static_cast<unsigned char>(table_code_careful(g.nb, code_scale));
   for (int i = 0; i < n; ++i) {
     double lo = (i - 0.5) / static_cast<double>(scale);
     double hi = (i + 0.5) / static_cast<double>(scale);
@@ -256,9 +269,9 @@ inline void build_table(Geom& g, int code_scale, unsigned char* tab) {
     // Inflate slightly for the rounding of the band arithmetic itself.
     const double blo = lo - (ka * lo + kb) * 1.01;
     const double bhi = hi + (ka * hi + kb) * 1.01;
-    unsigned char code = static_cast<unsigned char>(kCodeCareful);
+    unsigned char code = car;
     if (bhi <= g.sqr_rmin || blo >= g.sqr_rmax) {
-      code = static_cast<unsigned char>(kCodeReject);
+      code = rej;
     } else if (blo > g.sqr_rmin && bhi < g.sqr_rmax) {
       for (int b = 0; b < g.nb; ++b) {
         if (g.sqr_bins[b] <= blo && bhi < g.sqr_bins[b + 1]) {
@@ -272,7 +285,7 @@ inline void build_table(Geom& g, int code_scale, unsigned char* tab) {
 }
 
 inline void build_table(Geom& g, int code_scale, std::vector<unsigned char>& tab) {
-  tab.assign(kTableSize, static_cast<unsigned char>(kCodeCareful));
+  tab.assign(kTableSize, 0);
   build_table(g, code_scale, tab.data());
 }
 
@@ -290,11 +303,11 @@ struct TriShape {
 
 inline bool tri_shape(int nb, bool survey, bool sym, bool weighted, bool hg, int copies, int nsm, int64_t n_work,
                       int bound2, int bound3, TriShape* out) {
-  const long nbin = static_cast<long>(nb) * nb * nb;
+  const long nbp = hist_words(nb);
   const int elem = weighted ? 8 : 4;
   if (hg) copies = 1;
   copies = std::max(1, copies);
-  while (copies > 1 && static_cast<long>(copies) * nbin * elem > kHistSmemMax) copies >>= 1;
+  while (copies > 1 && static_cast<long>(copies) * nbp * elem > kHistSmemMax) copies >>= 1;
   const SmemLayout L = make_layout(nb, weighted, hg, copies);
   const int occ = triangles_occupancy(survey, sym, weighted, hg, static_cast<size_t>(L.total));
   if (occ <= 0) return false;
@@ -304,7 +317,8 @@ inline bool tri_shape(int nb, bool survey, bool sym, bool weighted, bool hg, int
   out->grid = static_cast<int>(std::min<int64_t>(static_cast<int64_t>(nsm) * occ, ctas_needed));
   out->kcap2 = ((std::max(bound2, 1) + 31) / 32) * 32;
   out->kcap3 = sym ? 0 : ((std::max(bound3, 1) + 31) / 32) * 32;
-  return true;
+  // The careful queue names list rows in 24 bits.
+  return out->kcap2 <= kListMax && out->kcap3 <= kListMax;
 }
 
 // Share of the launch's CTA-time spent idle at its end: CTA b ran from

@@ -87,7 +87,7 @@ __host__ __device__ inline SmemLayout make_layout(int nb, bool weighted, bool hi
   L.table = o;
   o += kTableSize;
   L.hist = o;
-  if (!hist_global) o = align16(o + hist_copies * nb * nb * nb * (weighted ? 8 : 4));
+  if (!hist_global) o = align16(o + hist_copies * hist_words(nb) * (weighted ? 8 : 4));
   L.slots = o;
   o += kWarps * static_cast<int>(sizeof(SlotTab));
   L.scratch = o;  // 8 bytes per lane: sink of non-counting reductions
@@ -205,22 +205,27 @@ __device__ __forceinline__ void add128(unsigned long long* w, long long v) {
 // v = p + (rho_l^2 + rho_j^2): three products and two adds instead of three
 // differences and three squares, and p itself is the quantity of the margin
 // test, |p| < 2 rho_j rho_l - M (|C - A - B| = |2 D_j.D_l| for the exact
-// sides). A candidate counts in bin `code` of the table when the margin test
-// holds; one that needs the careful or exact path ORs `rbit` (its row's bit
-// in the flag group) into the flag word of its column slot. The histogram
+// sides). Every candidate whose margin test holds is added at the address its
+// table code gives: its bin when the code is one, else one of the two sink
+// bins that end each (bin_j, bin_l) row of the CTA histogram (rejected,
+// careful), which nothing reads. So the body never tests the code for
+// "reject". A candidate whose code is "careful" or whose margin test fails
+// sets `rbit` (its row's bit in the flag group) in the lane's flag word; a
+// rejected one that fails the margin test (a nearly collinear triangle, rare)
+// is flagged too and the careful path rejects it again. The histogram
 // reduction is unconditional: a candidate that does not count adds to the
 // lane's own scratch word `dummy` instead, which keeps the loop free of the
 // branch a predicated atomic compiles to.
 //
 // Operands of the row bodies:
-//   %0-%3  flag words of column slots 0-3 (in/out)
-//   %4-%6  the row's offset d_j, %7 rho_j^2, %8 2 rho_j, %9 the row's key
-//          (histogram base + bin_j * nb^2 * code scale)
-//   %10 table scale, %11/%12 table address bias and last entry, %13 nb * code
-//   scale, %14 -M, %15 dummy address, %16 rbit, %17-%20 masks of column
-//   slots 0-3 (diagonal rows: 1 below the row's slot, l < j in it, 0 above)
-//   column c: %(21+5c)-%(23+5c) its offset scaled by -2, %(24+5c) rho_l,
-//   %(25+5c) its key (bin_l * nb * code scale)
+//   %0     the flag word of the row group (in/out)
+//   %1-%3  the row's offset d_j, %4 rho_j^2, %5 2 rho_j, %6 the row's key
+//          (histogram base + bin_j times its stride)
+//   %7 table scale, %8/%9 table address bias and last entry, %10 the careful
+//   code, %11 -M, %12 dummy address, %13 rbit
+//   column c: %(14+5c)-%(16+5c) its offset scaled by -2, %(17+5c) rho_l,
+//   %(18+5c) its key (bin_l times its stride)
+//   %19 (one-column bodies) the mask: 0 for a pair that is not to be counted
 // One asm statement per row lets all table loads issue before the first
 // reduction; in separate statements each load would wait behind the previous
 // candidate's reduction, which may touch the same shared-memory word as far
@@ -228,54 +233,49 @@ __device__ __forceinline__ void add128(unsigned long long* w, long long v) {
 #define NCORR_DECL(C)                                                     \
   ".reg .f32 pp" #C ", s" #C ", v" #C ", t" #C ", H" #C ";\n\t"           \
   ".reg .b32 y" #C ", ia" #C ", code" #C ", key" #C ", adr" #C ";\n\t"     \
-  ".reg .pred ok" #C ", upd" #C ", nco" #C ", wq" #C ";\n\t"
+  ".reg .pred upd" #C ", w" #C ";\n\t"
 #define NCORR_CLS(C, LX, LY, LZ, B)                  \
-  "mul.rn.f32 pp" #C ", %4, " LX ";\n\t"             \
-  "fma.rn.f32 pp" #C ", %5, " LY ", pp" #C ";\n\t"   \
-  "fma.rn.f32 pp" #C ", %6, " LZ ", pp" #C ";\n\t"   \
-  "fma.rn.f32 s" #C ", " B ", " B ", %7;\n\t"        \
+  "mul.rn.f32 pp" #C ", %1, " LX ";\n\t"             \
+  "fma.rn.f32 pp" #C ", %2, " LY ", pp" #C ";\n\t"   \
+  "fma.rn.f32 pp" #C ", %3, " LZ ", pp" #C ";\n\t"   \
+  "fma.rn.f32 s" #C ", " B ", " B ", %4;\n\t"        \
   "add.rn.f32 v" #C ", pp" #C ", s" #C ";\n\t"       \
-  "fma.rn.f32 y" #C ", v" #C ", %10, 0f4B000000;\n\t" \
-  "add.u32 ia" #C ", y" #C ", %11;\n\t"              \
-  "min.u32 ia" #C ", ia" #C ", %12;\n\t"             \
+  "fma.rn.f32 y" #C ", v" #C ", %7, 0f4B000000;\n\t" \
+  "add.u32 ia" #C ", y" #C ", %8;\n\t"               \
+  "min.u32 ia" #C ", ia" #C ", %9;\n\t"              \
   "ld.shared.u8 code" #C ", [ia" #C "];\n\t"
 // Column operand groups, expanded through NCORR_CLSX so that a group fills
 // the four column arguments of NCORR_CLS.
 #define NCORR_CLS_I(C, ...) NCORR_CLS(C, __VA_ARGS__)
 #define NCORR_CLSX(C, COLS) NCORR_CLS_I(C, COLS)
 #define NCORR_KEY(C, KL)                               \
-  "add.u32 key" #C ", %9, " KL ";\n\t"                 \
+  "add.u32 key" #C ", %6, " KL ";\n\t"                 \
   "add.u32 key" #C ", key" #C ", code" #C ";\n\t"      \
-  "selp.b32 adr" #C ", key" #C ", %15, upd" #C ";\n\t"
-#define NCORR_UPD(C, B, KL, Q)                                     \
+  "selp.b32 adr" #C ", key" #C ", %12, upd" #C ";\n\t"
+// upd: the margin test holds; w: careful code or failed margin test.
+#define NCORR_UPD(C, B, KL)                                        \
   "abs.f32 t" #C ", pp" #C ";\n\t"                                 \
-  "fma.rn.f32 H" #C ", %8, " B ", %14;\n\t"                        \
-  "setp.lt.u32 ok" #C ", code" #C ", %13;\n\t"                     \
-  "setp.lt.and.f32 upd" #C ", t" #C ", H" #C ", ok" #C ";\n\t"     \
-  "setp.ge.and.f32 nco" #C ", t" #C ", H" #C ", ok" #C ";\n\t"     \
-  "setp.eq.or.u32 wq" #C ", code" #C ", 255, nco" #C ";\n\t"       \
-  "@wq" #C " or.b32 " Q ", " Q ", %16;\n\t" NCORR_KEY(C, KL)
-#define NCORR_UPD_MASKED(C, B, KL, Q, M)                           \
+  "fma.rn.f32 H" #C ", %5, " B ", %11;\n\t"                        \
+  "setp.lt.f32 upd" #C ", t" #C ", H" #C ";\n\t"                   \
+  "setp.eq.or.u32 w" #C ", code" #C ", %10, !upd" #C ";\n\t" NCORR_KEY(C, KL)
+// The same under a mask: a masked-out pair neither counts nor flags.
+#define NCORR_UPD_MASKED(C, B, KL, M)                              \
   "abs.f32 t" #C ", pp" #C ";\n\t"                                 \
-  "fma.rn.f32 H" #C ", %8, " B ", %14;\n\t"                        \
-  "setp.ne.u32 inp" #C ", " M ", 0;\n\t"                           \
-  "setp.lt.u32 ok" #C ", code" #C ", %13;\n\t"                     \
-  "and.pred ok" #C ", ok" #C ", inp" #C ";\n\t"                    \
-  "setp.lt.and.f32 upd" #C ", t" #C ", H" #C ", ok" #C ";\n\t"     \
-  "setp.ge.and.f32 nco" #C ", t" #C ", H" #C ", ok" #C ";\n\t"     \
-  "setp.eq.and.u32 car" #C ", code" #C ", 255, inp" #C ";\n\t"     \
-  "or.pred wq" #C ", car" #C ", nco" #C ";\n\t"                    \
-  "@wq" #C " or.b32 " Q ", " Q ", %16;\n\t" NCORR_KEY(C, KL)
+  "fma.rn.f32 H" #C ", %5, " B ", %11;\n\t"                        \
+  "setp.ne.u32 inp, " M ", 0;\n\t"                                 \
+  "setp.lt.and.f32 upd" #C ", t" #C ", H" #C ", inp;\n\t"          \
+  "setp.eq.or.u32 w" #C ", code" #C ", %10, !upd" #C ";\n\t"       \
+  "and.pred w" #C ", w" #C ", inp;\n\t" NCORR_KEY(C, KL)
+#define NCORR_FLAG "@w0 or.b32 %0, %0, %13;\n\t"
 #define NCORR_RED(C) "red.shared.add.u32 [adr" #C "], 1;\n\t"
-#define NCORR_C0 "%21", "%22", "%23", "%24"
-#define NCORR_C1 "%26", "%27", "%28", "%29"
-#define NCORR_C2 "%31", "%32", "%33", "%34"
-#define NCORR_C3 "%36", "%37", "%38", "%39"
+#define NCORR_C0 "%14", "%15", "%16", "%17"
+#define NCORR_C1 "%19", "%20", "%21", "%22"
+#define NCORR_C2 "%24", "%25", "%26", "%27"
+#define NCORR_C3 "%29", "%30", "%31", "%32"
 #define NCORR_ROW_OPERANDS                                                                                      \
-  : "+r"(q0), "+r"(q1), "+r"(q2), "+r"(q3)                                                                     \
+  : "+r"(q)                                                                                                    \
   : "f"(r.x), "f"(r.y), "f"(r.z), "f"(r.a), "f"(r.a2r), "r"(r.key), "f"(k.tscale), "r"(k.tab_adj),             \
-    "r"(k.tab_last), "r"(k.nb_cs), "f"(k.hm), "r"(k.dummy), "r"(rbit), "r"(m0), "r"(m1), "r"(m2), "r"(m3),     \
-    "f"(c.l[0].x), "f"(c.l[0].y), \
+    "r"(k.tab_last), "r"(k.car), "f"(k.hm), "r"(k.dummy), "r"(rbit), "f"(c.l[0].x), "f"(c.l[0].y),             \
     "f"(c.l[0].z), "f"(c.l[0].w), "r"(c.k[0]), "f"(c.l[1].x), "f"(c.l[1].y), "f"(c.l[1].z), "f"(c.l[1].w),    \
     "r"(c.k[1]), "f"(c.l[2].x), "f"(c.l[2].y), "f"(c.l[2].z), "f"(c.l[2].w), "r"(c.k[2]), "f"(c.l[3].x),        \
     "f"(c.l[3].y), "f"(c.l[3].z), "f"(c.l[3].w), "r"(c.k[3])                                                   \
@@ -284,7 +284,7 @@ __device__ __forceinline__ void add128(unsigned long long* w, long long v) {
 // Constants of the candidate bodies, fixed per launch.
 struct BodyK {
   float tscale, hm;
-  unsigned tab_adj, tab_last, nb_cs, dummy;
+  unsigned tab_adj, tab_last, car, dummy;
 };
 // One row: offset, rho^2, 2 rho, key.
 struct RowV {
@@ -297,39 +297,46 @@ struct ColV {
   unsigned k[kReg];
 };
 
-// Four full candidates (column slots 0-3).
-__device__ __forceinline__ void row_full4(const RowV& r, const ColV& c, const BodyK& k, unsigned rbit, unsigned& q0,
-                                          unsigned& q1, unsigned& q2, unsigned& q3) {
-  const unsigned m0 = 1u, m1 = 1u, m2 = 1u, m3 = 1u;
-  asm volatile("{\n\t" NCORR_DECL(0) NCORR_DECL(1) NCORR_DECL(2) NCORR_DECL(3)
-               NCORR_CLSX(0, NCORR_C0) NCORR_CLSX(1, NCORR_C1) NCORR_CLSX(2, NCORR_C2) NCORR_CLSX(3, NCORR_C3)
-               NCORR_UPD(0, "%24", "%25", "%0") NCORR_UPD(1, "%29", "%30", "%1") NCORR_UPD(2, "%34", "%35", "%2")
-               NCORR_UPD(3, "%39", "%40", "%3")
-               NCORR_RED(0) NCORR_RED(1) NCORR_RED(2) NCORR_RED(3) "}" NCORR_ROW_OPERANDS);
+// Column slots 0..N-1 of one row, every pair one to count: N = 4 for the
+// rows past the diagonal tile (and every row of distinct lists), N = 1..3 for
+// the rows of the diagonal tile's block N against the blocks before it.
+template <int N>
+__device__ __forceinline__ void row_full(const RowV& r, const ColV& c, const BodyK& k, unsigned rbit, unsigned& q) {
+  if constexpr (N == 4) {
+    asm volatile("{\n\t" NCORR_DECL(0) NCORR_DECL(1) NCORR_DECL(2) NCORR_DECL(3)
+                 NCORR_CLSX(0, NCORR_C0) NCORR_CLSX(1, NCORR_C1) NCORR_CLSX(2, NCORR_C2) NCORR_CLSX(3, NCORR_C3)
+                 NCORR_UPD(0, "%17", "%18") NCORR_UPD(1, "%22", "%23") NCORR_UPD(2, "%27", "%28")
+                 NCORR_UPD(3, "%32", "%33")
+                 "or.pred w0, w0, w1;\n\tor.pred w2, w2, w3;\n\tor.pred w0, w0, w2;\n\t" NCORR_FLAG
+                 NCORR_RED(0) NCORR_RED(1) NCORR_RED(2) NCORR_RED(3) "}" NCORR_ROW_OPERANDS);
+  } else if constexpr (N == 3) {
+    asm volatile("{\n\t" NCORR_DECL(0) NCORR_DECL(1) NCORR_DECL(2)
+                 NCORR_CLSX(0, NCORR_C0) NCORR_CLSX(1, NCORR_C1) NCORR_CLSX(2, NCORR_C2)
+                 NCORR_UPD(0, "%17", "%18") NCORR_UPD(1, "%22", "%23") NCORR_UPD(2, "%27", "%28")
+                 "or.pred w0, w0, w1;\n\tor.pred w0, w0, w2;\n\t" NCORR_FLAG
+                 NCORR_RED(0) NCORR_RED(1) NCORR_RED(2) "}" NCORR_ROW_OPERANDS);
+  } else if constexpr (N == 2) {
+    asm volatile("{\n\t" NCORR_DECL(0) NCORR_DECL(1) NCORR_CLSX(0, NCORR_C0) NCORR_CLSX(1, NCORR_C1)
+                 NCORR_UPD(0, "%17", "%18") NCORR_UPD(1, "%22", "%23")
+                 "or.pred w0, w0, w1;\n\t" NCORR_FLAG NCORR_RED(0) NCORR_RED(1) "}" NCORR_ROW_OPERANDS);
+  } else {
+    static_assert(N == 1, "one to four column slots");
+    asm volatile("{\n\t" NCORR_DECL(0) NCORR_CLSX(0, NCORR_C0) NCORR_UPD(0, "%17", "%18") NCORR_FLAG
+                 NCORR_RED(0) "}" NCORR_ROW_OPERANDS);
+  }
 }
 
-// Four candidates with a mask each (diagonal rows of identical lists, pairs
-// l < j): masked-out candidates neither count nor flag.
-__device__ __forceinline__ void row_mask4(const RowV& r, const ColV& c, const BodyK& k, unsigned rbit, unsigned m0,
-                                          unsigned m1, unsigned m2, unsigned m3, unsigned& q0, unsigned& q1,
-                                          unsigned& q2, unsigned& q3) {
-  asm volatile("{\n\t.reg .pred inp0, inp1, inp2, inp3, car0, car1, car2, car3;\n\t"
-               NCORR_DECL(0) NCORR_DECL(1) NCORR_DECL(2) NCORR_DECL(3)
-               NCORR_CLSX(0, NCORR_C0) NCORR_CLSX(1, NCORR_C1) NCORR_CLSX(2, NCORR_C2) NCORR_CLSX(3, NCORR_C3)
-               NCORR_UPD_MASKED(0, "%24", "%25", "%0", "%17") NCORR_UPD_MASKED(1, "%29", "%30", "%1", "%18")
-               NCORR_UPD_MASKED(2, "%34", "%35", "%2", "%19") NCORR_UPD_MASKED(3, "%39", "%40", "%3", "%20")
-               NCORR_RED(0) NCORR_RED(1) NCORR_RED(2) NCORR_RED(3) "}" NCORR_ROW_OPERANDS);
-}
-
-// Two candidates with masks (column slots 0-1; diagonal rows of the first two
-// 32-row groups of a tile, where slots 2-3 hold no pair).
-__device__ __forceinline__ void row_mask2(const RowV& r, const ColV& c, const BodyK& k, unsigned rbit, unsigned m0,
-                                          unsigned m1, unsigned& q0, unsigned& q1, unsigned& q2, unsigned& q3) {
-  const unsigned m2 = 0u, m3 = 0u;
-  asm volatile("{\n\t.reg .pred inp0, inp1, car0, car1;\n\t" NCORR_DECL(0) NCORR_DECL(1)
-               NCORR_CLSX(0, NCORR_C0) NCORR_CLSX(1, NCORR_C1)
-               NCORR_UPD_MASKED(0, "%24", "%25", "%0", "%17") NCORR_UPD_MASKED(1, "%29", "%30", "%1", "%18")
-               NCORR_RED(0) NCORR_RED(1) "}" NCORR_ROW_OPERANDS);
+// One candidate under a mask, with a row of its own per lane: the pairs of a
+// diagonal 32-block, taken by rotation (column lane against row lane + d).
+__device__ __forceinline__ void row_rot1(const RowV& r, const float4& l, unsigned kl, const BodyK& k, unsigned rbit,
+                                         unsigned mask, unsigned& q) {
+  asm volatile("{\n\t.reg .pred inp;\n\t" NCORR_DECL(0) NCORR_CLSX(0, NCORR_C0)
+               NCORR_UPD_MASKED(0, "%17", "%18", "%19") NCORR_FLAG NCORR_RED(0) "}"
+               : "+r"(q)
+               : "f"(r.x), "f"(r.y), "f"(r.z), "f"(r.a), "f"(r.a2r), "r"(r.key), "f"(k.tscale), "r"(k.tab_adj),
+                 "r"(k.tab_last), "r"(k.car), "f"(k.hm), "r"(k.dummy), "r"(rbit), "f"(l.x), "f"(l.y), "f"(l.z),
+                 "f"(l.w), "r"(kl), "r"(mask)
+               : "memory");
 }
 
 // The weighted twin of one candidate: the same classification, then the
@@ -344,71 +351,47 @@ __device__ __forceinline__ void row_mask2(const RowV& r, const ColV& c, const Bo
 // total is exact however the adds interleave. Operands: %0 flag word,
 // %1-%3 d_j, %4 rho_j^2, %5 2 rho_j, %6-%8 -2 d_l, %9 rho_l, %10 row key,
 // %11 column key, %12 mask, %13 table scale, %14/%15 table bias and last
-// entry, %16 nb * code scale, %17 -M, %18 dummy, %19 row weight, %20 column
-// weight, %21 rbit.
-template <bool MASKED>
+// entry, %16 the careful code, %17 -M, %18 dummy, %19 row weight, %20 column
+// weight, %21 rbit. Rejected and careful codes address sink bins, as in the
+// count bodies.
 __device__ __forceinline__ void cand_wsum(const RowV& r, const float4& l, unsigned kl, unsigned in, const BodyK& k,
                                           float wrow, float wl, unsigned rbit, unsigned& q) {
-#define NCORR_WSUM_ASM(UPD)                                                                                  \
-  asm volatile("{\n\t.reg .pred inp, car;\n\t" NCORR_DECL(0)                                                 \
-               ".reg .f32 wp;\n\t.reg .b32 wi, whi, wold, wnew, wcy, adrh;\n\t"                             \
-               "mul.rn.f32 pp0, %1, %6;\n\t"                                                                 \
-               "fma.rn.f32 pp0, %2, %7, pp0;\n\t"                                                            \
-               "fma.rn.f32 pp0, %3, %8, pp0;\n\t"                                                            \
-               "fma.rn.f32 s0, %9, %9, %4;\n\t"                                                              \
-               "add.rn.f32 v0, pp0, s0;\n\t"                                                                 \
-               "fma.rn.f32 y0, v0, %13, 0f4B000000;\n\t"                                                     \
-               "add.u32 ia0, y0, %14;\n\t"                                                                   \
-               "min.u32 ia0, ia0, %15;\n\t"                                                                  \
-               "ld.shared.u8 code0, [ia0];\n\t" UPD                                                          \
-               "mul.rn.f32 wp, %19, %20;\n\t"                                                                \
-               "cvt.rni.s32.f32 wi, wp;\n\t"                                                                 \
-               "shr.s32 whi, wi, 31;\n\t"                                                                    \
-               "atom.shared.add.u32 wold, [adr0], wi;\n\t"                                                   \
-               "add.u32 wnew, wold, wi;\n\t"                                                                 \
-               "set.lt.u32.u32 wcy, wnew, wold;\n\t"                                                         \
-               "sub.u32 whi, whi, wcy;\n\t"                                                                  \
-               "add.u32 adrh, adr0, 4;\n\t"                                                                  \
-               "red.shared.add.u32 [adrh], whi;\n\t"                                                         \
-               "}"                                                                                           \
-               : "+r"(q)                                                                                     \
-               : "f"(r.x), "f"(r.y), "f"(r.z), "f"(r.a), "f"(r.a2r), "f"(l.x), "f"(l.y), "f"(l.z), "f"(l.w), \
-                 "r"(r.key), "r"(kl), "r"(in), "f"(k.tscale), "r"(k.tab_adj), "r"(k.tab_last), "r"(k.nb_cs), \
-                 "f"(k.hm), "r"(k.dummy), "f"(wrow), "f"(wl), "r"(rbit)                                      \
-               : "memory")
-#define NCORR_W_UPD                                                 \
-  "abs.f32 t0, pp0;\n\t"                                            \
-  "fma.rn.f32 H0, %5, %9, %17;\n\t"                                 \
-  "setp.lt.u32 ok0, code0, %16;\n\t"                                \
-  "setp.lt.and.f32 upd0, t0, H0, ok0;\n\t"                          \
-  "setp.ge.and.f32 nco0, t0, H0, ok0;\n\t"                          \
-  "setp.eq.or.u32 wq0, code0, 255, nco0;\n\t"                       \
-  "@wq0 or.b32 %0, %0, %21;\n\t"                                    \
-  "add.u32 key0, %10, %11;\n\t"                                     \
-  "add.u32 key0, key0, code0;\n\t"                                  \
-  "selp.b32 adr0, key0, %18, upd0;\n\t"
-#define NCORR_W_UPD_MASKED                                          \
-  "abs.f32 t0, pp0;\n\t"                                            \
-  "fma.rn.f32 H0, %5, %9, %17;\n\t"                                 \
-  "setp.ne.u32 inp, %12, 0;\n\t"                                    \
-  "setp.lt.u32 ok0, code0, %16;\n\t"                                \
-  "and.pred ok0, ok0, inp;\n\t"                                     \
-  "setp.lt.and.f32 upd0, t0, H0, ok0;\n\t"                          \
-  "setp.ge.and.f32 nco0, t0, H0, ok0;\n\t"                          \
-  "setp.eq.and.u32 car, code0, 255, inp;\n\t"                       \
-  "or.pred wq0, car, nco0;\n\t"                                     \
-  "@wq0 or.b32 %0, %0, %21;\n\t"                                    \
-  "add.u32 key0, %10, %11;\n\t"                                     \
-  "add.u32 key0, key0, code0;\n\t"                                  \
-  "selp.b32 adr0, key0, %18, upd0;\n\t"
-  if (MASKED) {
-    NCORR_WSUM_ASM(NCORR_W_UPD_MASKED);
-  } else {
-    NCORR_WSUM_ASM(NCORR_W_UPD);
-  }
-#undef NCORR_W_UPD_MASKED
-#undef NCORR_W_UPD
-#undef NCORR_WSUM_ASM
+  asm volatile("{\n\t.reg .pred inp;\n\t" NCORR_DECL(0)
+               ".reg .f32 wp;\n\t.reg .b32 wi, whi, wold, wnew, wcy, adrh;\n\t"
+               "mul.rn.f32 pp0, %1, %6;\n\t"
+               "fma.rn.f32 pp0, %2, %7, pp0;\n\t"
+               "fma.rn.f32 pp0, %3, %8, pp0;\n\t"
+               "fma.rn.f32 s0, %9, %9, %4;\n\t"
+               "add.rn.f32 v0, pp0, s0;\n\t"
+               "fma.rn.f32 y0, v0, %13, 0f4B000000;\n\t"
+               "add.u32 ia0, y0, %14;\n\t"
+               "min.u32 ia0, ia0, %15;\n\t"
+               "ld.shared.u8 code0, [ia0];\n\t"
+               "abs.f32 t0, pp0;\n\t"
+               "fma.rn.f32 H0, %5, %9, %17;\n\t"
+               "setp.ne.u32 inp, %12, 0;\n\t"
+               "setp.lt.and.f32 upd0, t0, H0, inp;\n\t"
+               "setp.eq.or.u32 w0, code0, %16, !upd0;\n\t"
+               "and.pred w0, w0, inp;\n\t"
+               "@w0 or.b32 %0, %0, %21;\n\t"
+               "add.u32 key0, %10, %11;\n\t"
+               "add.u32 key0, key0, code0;\n\t"
+               "selp.b32 adr0, key0, %18, upd0;\n\t"
+               "mul.rn.f32 wp, %19, %20;\n\t"
+               "cvt.rni.s32.f32 wi, wp;\n\t"
+               "shr.s32 whi, wi, 31;\n\t"
+               "atom.shared.add.u32 wold, [adr0], wi;\n\t"
+               "add.u32 wnew, wold, wi;\n\t"
+               "set.lt.u32.u32 wcy, wnew, wold;\n\t"
+               "sub.u32 whi, whi, wcy;\n\t"
+               "add.u32 adrh, adr0, 4;\n\t"
+               "red.shared.add.u32 [adrh], whi;\n\t"
+               "}"
+               : "+r"(q)
+               : "f"(r.x), "f"(r.y), "f"(r.z), "f"(r.a), "f"(r.a2r), "f"(l.x), "f"(l.y), "f"(l.z), "f"(l.w),
+                 "r"(r.key), "r"(kl), "r"(in), "f"(k.tscale), "r"(k.tab_adj), "r"(k.tab_last), "r"(k.car),
+                 "f"(k.hm), "r"(k.dummy), "f"(wrow), "f"(wl), "r"(rbit)
+               : "memory");
 }
 
 #undef NCORR_ROW_OPERANDS
@@ -417,6 +400,7 @@ __device__ __forceinline__ void cand_wsum(const RowV& r, const float4& l, unsign
 #undef NCORR_C2
 #undef NCORR_C3
 #undef NCORR_RED
+#undef NCORR_FLAG
 #undef NCORR_UPD_MASKED
 #undef NCORR_UPD
 #undef NCORR_KEY
@@ -495,14 +479,18 @@ __device__ __forceinline__ void settle_exact(const KArgs& a, const ExactEntry& e
 struct Cold {
   const KArgs* a;
   ListView l2, l3;
-  unsigned long long* queue;  // this warp's (j, l) queue (global)
+  unsigned long long* queue;  // this warp's careful queue (global)
   ExactEntry* xbuf;           // this warp's buffer of uncertain candidates (global)
   const float* e2lo;
   const float* e2hi;
-  unsigned char* hist_s;  // this lane's copy of the CTA histogram
+  const unsigned char* tab;  // the bin table (shared memory)
+  unsigned char* hist_s;     // this lane's copy of the CTA histogram
   HistOut hist;           // the current item's global histogram
-  int qn, xn;
+  int xn;
   int nb, cs, ai;  // ai: the anchor's position in the work queue
+  // Histogram strides of bin_j and bin_l: bytes in the CTA histogram (with
+  // its sink bins), bins in the global one.
+  unsigned kjm, klm;
   float wa;
   unsigned lane, lt_mask;
   unsigned long long n_exact_tri, n_queued, n_flag_rows;
@@ -556,77 +544,104 @@ __device__ __forceinline__ void hist_add(unsigned char* hist_s, const HistOut& h
   }
 }
 
-// Settles the queued candidates, 32 per round: the explicit FP32 band and the
-// margin test of the triangle decide most; the rest go to the exact buffer.
+// Careful queue entries: a lane's flag word of one row group in the high
+// half, and in the low half  base << 8 | kind << 5 | lane.
+//   kind n < 4: bit o is row base + o against column slots 0..n of the tile
+//               at lb, that is columns lb + 32 s + lane;
+//   kind 4:     the diagonal block at base; bit d - 1 is row
+//               base + ((lane + d) & 31) against column base + lane.
+constexpr unsigned kKindRot = 4;
+
+// Settles the careful queue's entries of the tile at lb, one candidate per
+// lane and round: the explicit FP32 band and the margin test of the triangle
+// decide most; the rest go to the exact buffer. Flagged columns at or past
+// k3 (the padding of the last tile) are skipped.
 template <bool SURVEY, bool WEIGHTED, bool HG>
-__device__ __noinline__ void cold_drain(Cold& c) {
+__device__ __noinline__ void cold_drain(Cold& c, int lb, int k3, int qn) {
   const KArgs& a = *c.a;
   const Geom& g = a.g;
   const int nb = c.nb;
   __syncwarp();
-  for (int q0 = 0; q0 < c.qn; q0 += 32) {
-    const int qi = q0 + static_cast<int>(c.lane);
-    bool exact = false;
-    ExactEntry xe;
-    if (qi < c.qn) {
-      const unsigned long long pr = c.queue[qi];
-      const int j = static_cast<int>(pr & 0xffffffffu);
-      const int l = static_cast<int>(pr >> 32);
-      const float4 ej = c.l2.e[j];
-      const unsigned mj = c.l2.m[j];
-      const float4 el = c.l3.e[l];
-      const unsigned ml = c.l3.m[l];
-      const float dx = ej.x - el.x, dy = ej.y - el.y, dz = ej.z - el.z;
-      const float v = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-      const unsigned key_jl = ((mj & 0xffu) * nb * nb + (ml & 0xffu) * nb);
-      unsigned code = careful_code(v, c.e2lo, c.e2hi, nb, g.ka, g.kb);
-      if (code < static_cast<unsigned>(nb)) {
-        if (!heron_clean(v, __fmul_rn(ej.w, ej.w), 2.0f * ej.w, el.w, g.hm)) code = kCodeExact;
-      }
-      if (code == kCodeExact) {
-        ++c.n_exact_tri;
-        exact = true;
-        xe.ai = c.ai;
-        xe.pj = c.l2.p[j];
-        xe.pl = c.l3.p[l];
-        xe.meta = (mj >> 8) | ((ml >> 8) << 5) | ((mj & 0xffu) << 10) | ((ml & 0xffu) << 18);
-      } else if (code < static_cast<unsigned>(nb)) {
-        const float wprod = WEIGHTED ? (c.wa * c.l2.w[j]) * c.l3.w[l] * a.wscale : 0.0f;
-        hist_add<WEIGHTED, HG>(c.hist_s, c.hist, (key_jl + code) * c.cs, wprod);
-      }
+  for (int e0 = 0; e0 < qn; e0 += 32) {
+    const int ei = e0 + static_cast<int>(c.lane);
+    unsigned bits = 0, tag = 0;
+    if (ei < qn) {
+      const unsigned long long en = c.queue[ei];
+      bits = static_cast<unsigned>(en >> 32);
+      tag = static_cast<unsigned>(en);
+      c.n_flag_rows += static_cast<unsigned>(__popc(bits));
     }
-    const unsigned xbal = __ballot_sync(0xffffffffu, exact);
-    if (c.xn + __popc(xbal) > 32) cold_flush_exact<SURVEY, WEIGHTED>(c);
-    if (exact) c.xbuf[c.xn + __popc(xbal & c.lt_mask)] = xe;
-    c.xn += __popc(xbal);
-    __syncwarp();
-  }
-  c.qn = 0;
-  __syncwarp();
-}
-
-// Queues the candidates flagged in a group of rows: bit o of the flag word of
-// column slot s stands for row jb + o against column lb + 32 s + lane.
-template <bool SURVEY, bool WEIGHTED, bool HG>
-__device__ __noinline__ void cold_enqueue(Cold& c, int jb, int lb, unsigned q0, unsigned q1, unsigned q2,
-                                          unsigned q3) {
-  unsigned rows = __reduce_or_sync(0xffffffffu, q0 | q1 | q2 | q3);
-  const unsigned q[4] = {q0, q1, q2, q3};
-  while (rows) {
-    const int o = __ffs(rows) - 1;
-    rows &= rows - 1u;
-    if (c.qn > kQueueCap - kTile) cold_drain<SURVEY, WEIGHTED, HG>(c);
-    ++c.n_flag_rows;
-#pragma unroll
-    for (int s = 0; s < kReg; ++s) {
-      const bool want = (q[s] >> o) & 1u;
-      const unsigned bal = __ballot_sync(0xffffffffu, want);
-      if (want)
-        c.queue[c.qn + __popc(bal & c.lt_mask)] =
-            static_cast<unsigned long long>(jb + o) |
-            (static_cast<unsigned long long>(lb + 32 * s + static_cast<int>(c.lane)) << 32);
-      c.qn += __popc(bal);
-      c.n_queued += __popc(bal);
+    const unsigned kind = (tag >> 5) & 7u, el_lane = tag & 31u;
+    const int base = static_cast<int>(tag >> 8);
+    const int nsl = kind == kKindRot ? 1 : static_cast<int>(kind) + 1;
+    int s = 0;
+    while (__any_sync(0xffffffffu, bits != 0u)) {
+      bool exact = false;
+      ExactEntry xe;
+      if (bits) {
+        const int o = __ffs(bits) - 1;
+        int j, l;
+        if (kind == kKindRot) {
+          j = base + static_cast<int>((el_lane + static_cast<unsigned>(o) + 1u) & 31u);
+          l = base + static_cast<int>(el_lane);
+        } else {
+          j = base + o;
+          l = lb + 32 * s + static_cast<int>(el_lane);
+        }
+        if (++s == nsl) {
+          s = 0;
+          bits &= bits - 1u;
+        }
+        const float4 ej = c.l2.e[j];
+        const float4 el = c.l3.e[min(l, k3 - 1)];
+        // A row's bit stands for all its column slots: keep the candidates
+        // the body itself flagged (its classification, recomputed with the
+        // same operations), not the ones it counted or rejected.
+        bool flagged = l < k3;
+        if (flagged && kind != kKindRot) {
+          RowV r;
+          r.x = ej.x;
+          r.y = ej.y;
+          r.z = ej.z;
+          r.a = __fmul_rn(ej.w, ej.w);
+          r.a2r = 2.0f * ej.w;
+          r.key = 0;
+          const float4 lc = make_float4(-2.0f * el.x, -2.0f * el.y, -2.0f * el.z, el.w);
+          unsigned bc;
+          bool clean;
+          cand_classify(r, lc, c.tab, g.tab_scale, g.tab_n, g.hm, &bc, &clean);
+          const unsigned car = table_code_careful(nb, c.cs);
+          flagged = bc == car || (!clean && (!HG || bc < static_cast<unsigned>(nb * c.cs)));
+        }
+        if (flagged) {
+          ++c.n_queued;
+          const unsigned mj = c.l2.m[j];
+          const unsigned ml = c.l3.m[l];
+          const float dx = ej.x - el.x, dy = ej.y - el.y, dz = ej.z - el.z;
+          const float v = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+          unsigned code = careful_code(v, c.e2lo, c.e2hi, nb, g.ka, g.kb);
+          if (code < static_cast<unsigned>(nb)) {
+            if (!heron_clean(v, __fmul_rn(ej.w, ej.w), 2.0f * ej.w, el.w, g.hm)) code = kCodeExact;
+          }
+          if (code == kCodeExact) {
+            ++c.n_exact_tri;
+            exact = true;
+            xe.ai = c.ai;
+            xe.pj = c.l2.p[j];
+            xe.pl = c.l3.p[l];
+            xe.meta = (mj >> 8) | ((ml >> 8) << 5) | ((mj & 0xffu) << 10) | ((ml & 0xffu) << 18);
+          } else if (code < static_cast<unsigned>(nb)) {
+            const float wprod = WEIGHTED ? (c.wa * c.l2.w[j]) * c.l3.w[l] * a.wscale : 0.0f;
+            const unsigned key = (mj & 0xffu) * c.kjm + (ml & 0xffu) * c.klm + code * static_cast<unsigned>(c.cs);
+            hist_add<WEIGHTED, HG>(c.hist_s, c.hist, key, wprod);
+          }
+        }
+      }
+      const unsigned xbal = __ballot_sync(0xffffffffu, exact);
+      if (c.xn + __popc(xbal) > 32) cold_flush_exact<SURVEY, WEIGHTED>(c);
+      if (exact) c.xbuf[c.xn + __popc(xbal & c.lt_mask)] = xe;
+      c.xn += __popc(xbal);
+      __syncwarp();
     }
   }
   __syncwarp();
@@ -645,26 +660,30 @@ static __device__ __noinline__ unsigned cold_pair_exact(const Geom* g, const dou
 // two 32-bit words; taking them one at a time can split one thread's
 // low-word and high-word additions between this drain and a later one, but
 // the sum over all drains plus what remains is still exact (every carry is
-// added to the high word by the thread that caused it).
+// added to the high word by the thread that caused it). Bin i of the global
+// histogram is word (i / nb) * (nb + 2) + i % nb of a copy; the sink bins are
+// left alone (their values are never used, so wrapping is harmless).
 template <bool WEIGHTED>
-__device__ __noinline__ void drain_hist(const KArgs* a, unsigned char* hist_s, int nbin, int copies, unsigned owner,
+__device__ __noinline__ void drain_hist(const KArgs* a, unsigned char* hist_s, int nb, int copies, unsigned owner,
                                         int t0, int stride) {
   if (owner == 0 || owner == kSlotLocked) return;
   const HistOut out = a->items[owner - 1].hist;
+  const int nbin = nb * nb * nb, nbp = hist_words(nb);
   for (int i = t0; i < nbin; i += stride) {
+    const int pi = (i / nb) * hist_row(nb) + i % nb;
     if (WEIGHTED) {
       unsigned* h = reinterpret_cast<unsigned*>(hist_s);
       long long v = 0;
       for (int cp = 0; cp < copies; ++cp) {
-        const unsigned lo = atomicExch(&h[2 * (cp * nbin + i)], 0u);
-        const unsigned hi = atomicExch(&h[2 * (cp * nbin + i) + 1], 0u);
+        const unsigned lo = atomicExch(&h[2 * (cp * nbp + pi)], 0u);
+        const unsigned hi = atomicExch(&h[2 * (cp * nbp + pi) + 1], 0u);
         v += static_cast<long long>((static_cast<unsigned long long>(hi) << 32) | lo);
       }
       if (v) add128(&out.wsum[2 * i], v);
     } else {
       unsigned* h = reinterpret_cast<unsigned*>(hist_s);
       unsigned long long v = 0;
-      for (int cp = 0; cp < copies; ++cp) v += atomicExch(&h[cp * nbin + i], 0u);
+      for (int cp = 0; cp < copies; ++cp) v += atomicExch(&h[cp * nbp + pi], 0u);
       if (v) atomicAdd(&out.counts[i], v);
     }
   }
@@ -693,13 +712,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_triangles(KArgs a) {
   unsigned char* tab = smem + L.table;
   unsigned char* hist_s = smem + L.hist;
   SlotTab& st = reinterpret_cast<SlotTab*>(smem + L.slots)[warp];
-  const int nbin = nb * nb * nb;
+  const int nbp = hist_words(nb);  // words of one copy of the CTA histogram, sinks included
   const int copies = HG ? 1 : a.hist_copies;
   // This lane's copy of the CTA histogram: lanes that hit one bin in the same
   // instruction spread over the copies.
-  const unsigned copy_off = static_cast<unsigned>((lane & (copies - 1)) * nbin * (WEIGHTED ? 8 : 4));
+  const unsigned copy_off = static_cast<unsigned>((lane & (copies - 1)) * nbp * (WEIGHTED ? 8 : 4));
   const int cs = a.code_scale;
   const unsigned nb_cs = static_cast<unsigned>(nb * cs);
+  const unsigned car = table_code_careful(nb, cs);
   const int group = a.sub_j;
 
   for (int i = tid; i <= nb; i += kThreads) {
@@ -709,7 +729,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_triangles(KArgs a) {
   }
   for (int i = tid; i < g.tab_n; i += kThreads) tab[i] = a.table[i];
   if (!HG) {
-    for (int i = tid; i < nbin * copies; i += kThreads) {
+    for (int i = tid; i < nbp * copies; i += kThreads) {
       if (WEIGHTED)
         reinterpret_cast<long long*>(hist_s)[i] = 0;
       else
@@ -752,10 +772,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_triangles(KArgs a) {
   c.xbuf = a.slab_x + gw * 32;
   c.e2lo = s_e2lo;
   c.e2hi = s_e2hi;
+  c.tab = tab;
   c.hist_s = hist_s + copy_off;
   c.hist.counts = nullptr;
   c.hist.wsum = nullptr;
-  c.qn = 0;
   c.xn = 0;
   c.nb = nb;
   c.cs = cs;
@@ -777,13 +797,18 @@ __global__ void __launch_bounds__(kThreads, 1) k_triangles(KArgs a) {
     const unsigned tab_sh = static_cast<unsigned>(__cvta_generic_to_shared(tab));
     bk.tab_adj = tab_sh - 0x4B000000u;
     bk.tab_last = tab_sh + static_cast<unsigned>(g.tab_n - 1);
-    bk.nb_cs = nb_cs;
+    bk.car = car;
     bk.dummy = static_cast<unsigned>(__cvta_generic_to_shared(smem + L.scratch)) + 8u * lane;
     bk.tscale = g.tab_scale;
     bk.hm = g.hm;
   }
   const unsigned hist_sh = static_cast<unsigned>(__cvta_generic_to_shared(hist_s)) + copy_off;
-  const unsigned kj_mul = static_cast<unsigned>(nb * nb * cs);
+  // Strides of bin_l and bin_j: the CTA histogram's rows of nb + 2 bins
+  // (bytes), or the global histogram's nb (bins).
+  const unsigned kl_mul = HG ? static_cast<unsigned>(nb) : static_cast<unsigned>(hist_row(nb) * cs);
+  const unsigned kj_mul = static_cast<unsigned>(nb) * kl_mul;
+  c.kjm = kj_mul;
+  c.klm = kl_mul;
   unsigned held = 0;  // owner code of the histogram binding this warp holds (0: none)
 
   for (;;) {
@@ -828,7 +853,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_triangles(KArgs a) {
         }
         if (r == 2) {
           old_owner = __shfl_sync(FULL, old_owner, 0);
-          if (!HG) drain_hist<WEIGHTED>(a.self, hist_s, nbin, copies, old_owner, lane, 32);
+          if (!HG) drain_hist<WEIGHTED>(a.self, hist_s, nb, copies, old_owner, lane, 32);
           __syncwarp();
           if (lane == 0) {
             s_since = 0u;
@@ -978,7 +1003,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_triangles(KArgs a) {
             unsigned code = table_code(v, tab, g.tab_scale, g.tab_n);
             if (code < nb_cs) {
               code /= cs;
-            } else if (code == kCodeCareful) {
+            } else if (code == car) {
               code = careful_code(v, s_e2lo, s_e2hi, nb, g.ka, g.kb);
             }
             if (code == kCodeExact) {
@@ -1044,7 +1069,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_triangles(KArgs a) {
         if (lane == 0) old = atomicAdd(&s_since, units);
         old = __shfl_sync(FULL, old, 0);
         if (!HG && (old >> kSinceDrainBits) != ((old + units) >> kSinceDrainBits))
-          drain_hist<WEIGHTED>(a.self, hist_s, nbin, copies, held, lane, 32);
+          drain_hist<WEIGHTED>(a.self, hist_s, nb, copies, held, lane, 32);
       }
       // Columns are held as (-2 d_l, rho_l); the padding (0, rho = 1e18)
       // gives v = 1e36 and is rejected by the table for every row.
@@ -1056,7 +1081,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_triangles(KArgs a) {
         if (l < k3) {
           const float4 e = l3.e[l];
           col.l[r] = make_float4(-2.0f * e.x, -2.0f * e.y, -2.0f * e.z, e.w);
-          col.k[r] = (l3.m[l] & 0xffu) * nb_cs;
+          col.k[r] = (l3.m[l] & 0xffu) * kl_mul;
           wl[r] = WEIGHTED ? l3.w[l] : 0.0f;
         } else {
           col.l[r] = make_float4(0.0f, 0.0f, 0.0f, 1.0e18f);
@@ -1074,83 +1099,110 @@ __global__ void __launch_bounds__(kThreads, 1) k_triangles(KArgs a) {
         r.key = HG ? (m & 0xffu) * kj_mul : (m & 0xffu) * kj_mul + hist_sh;
         return r;
       };
-      // Weighted and global-histogram rows: one candidate at a time, each
-      // with its mask (diagonal rows; 1 elsewhere).
-      auto row_slow = [&](const RowV& r, float wj, unsigned rbit, const unsigned (&m)[kReg], unsigned& q0,
-                          unsigned& q1, unsigned& q2, unsigned& q3) {
-        auto one = [&](auto s_tag, unsigned& q) {
-          constexpr int S = decltype(s_tag)::value;
-          const unsigned ins = m[S];
-          if (HG) {
-            unsigned code;
-            bool clean;
-            cand_classify(r, col.l[S], tab, g.tab_scale, g.tab_n, bk.hm, &code, &clean);
-            const bool ok = code < nb_cs && ins;
-            const bool careful = (code == kCodeCareful || (code < nb_cs && !clean)) && ins;
-            if (ok && clean)
-              hist_add<WEIGHTED, true>(hist_s, c.hist, r.key + col.k[S] + code, (wa * wj * wsc) * wl[S]);
-            if (careful) q |= rbit;
-          } else if (WEIGHTED) {
-            cand_wsum<true>(r, col.l[S], col.k[S], ins, bk, wa * wj * wsc, wl[S], rbit, q);
-          }
-        };
-        one(std::integral_constant<int, 0>(), q0);
-        one(std::integral_constant<int, 1>(), q1);
-        one(std::integral_constant<int, 2>(), q2);
-        one(std::integral_constant<int, 3>(), q3);
+      // The careful queue: entries of this tile, settled when it fills and
+      // at the end of the tile (format at kKindRot).
+      int qn = 0;
+      auto enqueue = [&](unsigned q, unsigned tag) {
+        const unsigned bal = __ballot_sync(FULL, q != 0u);
+        if (bal == 0u) return;
+        if (qn + 32 > kQueueCap) {
+          cold_drain<SURVEY, WEIGHTED, HG>(c, lb, k3, qn);
+          qn = 0;
+        }
+        if (q) c.queue[qn + __popc(bal & lt_mask)] = (static_cast<unsigned long long>(q) << 32) | tag;
+        qn += __popc(bal);
       };
-      // Rows [jb, je) of one flag group, all of one kind: full rows, or
-      // diagonal rows (SYM: rows of the column tile itself, whose slot
-      // S = (j - lb) / 32 is masked by l < j and the slots above it empty).
-      auto rows = [&](int jb, int je, auto diag_tag, unsigned& q0, unsigned& q1, unsigned& q2, unsigned& q3) {
-        constexpr bool DIAG = decltype(diag_tag)::value;
-        const int S = (jb - lb) >> 5;  // diagonal rows: the row's own slot (uniform in the group)
-        float4 en = l2.e[jb];
-        unsigned mn = l2.m[jb];
-#pragma unroll(DIAG ? 1 : 2)
+      // Weighted and global-histogram candidates, one at a time.
+      auto cand_slow = [&](const RowV& r, const float4& cl, unsigned ck, float cw, unsigned in, float wj,
+                           unsigned rbit, unsigned& q) {
+        if (HG) {
+          unsigned code;
+          bool clean;
+          cand_classify(r, cl, tab, g.tab_scale, g.tab_n, bk.hm, &code, &clean);
+          const bool ok = code < nb_cs && in;
+          const bool careful = (code == car || (code < nb_cs && !clean)) && in;
+          if (ok && clean) hist_add<WEIGHTED, true>(hist_s, c.hist, r.key + ck + code, (wa * wj * wsc) * cw);
+          if (careful) q |= rbit;
+        } else if (WEIGHTED) {
+          cand_wsum(r, cl, ck, in, bk, wa * wj * wsc, cw, rbit, q);
+        }
+      };
+      // Rows [jb, je) of one flag group against column slots 0..N-1.
+      auto rows = [&](int jb, int je, auto n_tag, unsigned& q) {
+        constexpr int N = decltype(n_tag)::value;
+#pragma unroll(N == kReg ? 2 : 1)
         for (int j = jb; j < je; ++j) {
-          const float4 e = en;
-          const unsigned m = mn;
-          const int jn = min(j + 1, k2 - 1);
-          en = l2.e[jn];
-          mn = l2.m[jn];
-          const RowV r = make_row(e, m);
+          const RowV r = make_row(l2.e[j], l2.m[j]);
           const unsigned rbit = 1u << (j - jb);
-          unsigned mk[kReg] = {1u, 1u, 1u, 1u};
-          if (DIAG) {
-            const unsigned in = ((j - lb) & 31) > lane ? 1u : 0u;
-#pragma unroll
-            for (int s = 0; s < kReg; ++s) mk[s] = s < S ? 1u : (s == S ? in : 0u);
-          }
           if (WEIGHTED || HG) {
             const float wj = WEIGHTED ? l2.w[j] : 0.0f;
-            row_slow(r, wj, rbit, mk, q0, q1, q2, q3);
-          } else if (!DIAG) {
-            row_full4(r, col, bk, rbit, q0, q1, q2, q3);
-          } else if (S < 2) {
-            row_mask2(r, col, bk, rbit, mk[0], mk[1], q0, q1, q2, q3);
+#pragma unroll
+            for (int s = 0; s < N; ++s) cand_slow(r, col.l[s], col.k[s], wl[s], 1u, wj, rbit, q);
           } else {
-            row_mask4(r, col, bk, rbit, mk[0], mk[1], mk[2], mk[3], q0, q1, q2, q3);
+            row_full<N>(r, col, bk, rbit, q);
           }
         }
       };
-      // Groups of `group` rows (8, 16 or 32, so a group never straddles a
-      // 32-row slot boundary of the diagonal); after each, the flagged
-      // candidates are queued.
+      // Rows [j0, j1) against column slots 0..N-1, in groups of `group` rows
+      // (8, 16 or 32: a group never straddles a 32-row block), each group's
+      // flag words queued after it.
+      auto groups = [&](int j0, int j1, auto n_tag) {
+        constexpr int N = decltype(n_tag)::value;
 #pragma unroll 1
-      for (int jb = jfirst; jb < k2; jb += group) {
-        const int je = min(jb + group, k2);
-        unsigned q0 = 0, q1 = 0, q2 = 0, q3 = 0;
-        if (!SYM || jb >= lb + kTile)
-          rows(jb, je, std::false_type(), q0, q1, q2, q3);
-        else
-          rows(jb, je, std::true_type(), q0, q1, q2, q3);
-        if (__any_sync(FULL, (q0 | q1 | q2 | q3) != 0))
-          cold_enqueue<SURVEY, WEIGHTED, HG>(c, jb, lb, q0, q1, q2, q3);
+        for (int jb = j0; jb < j1; jb += group) {
+          const int je = min(jb + group, j1);
+          unsigned q = 0;
+          rows(jb, je, n_tag, q);
+          enqueue(q, (static_cast<unsigned>(jb) << 8) | (static_cast<unsigned>(N - 1) << 5) |
+                         static_cast<unsigned>(lane));
+        }
+      };
+      if (SYM) {
+        // The diagonal tile, pairs l < j of its rows: block S (rows
+        // lb + 32 S ..) against the column slots before it, then the pairs
+        // inside the block by rotation, lane's column against row
+        // lane + d (mod 32) for d = 1..16 (d = 16 in lanes 0-15 only), so
+        // that no lane evaluates a pair that is not one.
+        const int m = min(kTile, k2 - lb);
+#pragma unroll 1
+        for (int S = 0; S * 32 < m; ++S) {
+          const int bb = lb + 32 * S, be = min(bb + 32, k2);
+          if (S == 1) groups(bb, be, std::integral_constant<int, 1>());
+          if (S == 2) groups(bb, be, std::integral_constant<int, 2>());
+          if (S == 3) groups(bb, be, std::integral_constant<int, 3>());
+          float4 cl = col.l[0];
+          unsigned ck = col.k[0];
+          float cw = wl[0];
+#pragma unroll
+          for (int s = 1; s < kReg; ++s) {
+            if (S == s) {
+              cl = col.l[s];
+              ck = col.k[s];
+              cw = wl[s];
+            }
+          }
+          const bool cval = bb + lane < k2;
+          unsigned qd = 0;
+#pragma unroll 2
+          for (int d = 1; d <= 16; ++d) {
+            const int rr = bb + ((lane + d) & 31);
+            const unsigned in = (cval && rr < k2 && (d < 16 || lane < 16)) ? 1u : 0u;
+            const int rl = min(rr, k2 - 1);
+            const RowV r = make_row(l2.e[rl], l2.m[rl]);
+            const unsigned rbit = 1u << (d - 1);
+            if (WEIGHTED || HG)
+              cand_slow(r, cl, ck, cw, in, WEIGHTED ? l2.w[rl] : 0.0f, rbit, qd);
+            else
+              row_rot1(r, cl, ck, bk, rbit, in, qd);
+          }
+          enqueue(qd, (static_cast<unsigned>(bb) << 8) | (kKindRot << 5) | static_cast<unsigned>(lane));
+        }
+        groups(lb + kTile, k2, std::integral_constant<int, kReg>());
+      } else {
+        groups(0, k2, std::integral_constant<int, kReg>());
       }
+      if (qn > 0) cold_drain<SURVEY, WEIGHTED, HG>(c, lb, k3, qn);
     }
-    // Queue entries refer to this anchor's lists: settle them now.
-    if (c.qn > 0) cold_drain<SURVEY, WEIGHTED, HG>(c);
   }
   if (lane == 0 && held) atomicAdd(&s_slot, ~0ull);
   cold_flush_exact<SURVEY, WEIGHTED>(c);
@@ -1163,17 +1215,17 @@ __global__ void __launch_bounds__(kThreads, 1) k_triangles(KArgs a) {
   if (!HG) {
     // Every warp has left: drain what the CTA histogram holds.
     const unsigned owner = static_cast<unsigned>(s_slot >> 32);
-    drain_hist<WEIGHTED>(a.self, hist_s, nbin, copies, owner, tid, kThreads);
+    drain_hist<WEIGHTED>(a.self, hist_s, nb, copies, owner, tid, kThreads);
   }
   if (a.stats) {
     atomicAdd(&a.stats[0], c.n_exact_tri);
     atomicAdd(&a.stats[1], c.n_exact_pair);
+    atomicAdd(&a.stats[5], c.n_flag_rows);
+    atomicAdd(&a.stats[6], c.n_queued);
     if (lane == 0) {
       atomicAdd(&a.stats[2], c.n_anchor);
       atomicAdd(&a.stats[3], c.n_pairs);
       atomicAdd(&a.stats[4], c.n_evals);
-      atomicAdd(&a.stats[5], c.n_flag_rows);
-      atomicAdd(&a.stats[6], c.n_queued);
     }
   }
 }

@@ -57,7 +57,8 @@ typedef struct ncorr_stats {
   uint64_t n_exact_pairs;  /* neighbours settled by the FP64 path */
   uint64_t n_exact_tris;   /* triangles (rppi: pairs) settled by the FP64 path */
   uint64_t triangles;      /* sum of the full histogram (count mode) */
-  uint64_t n_flagged_rows; /* neighbour rows re-examined for uncertain candidates */
+  uint64_t n_flagged_rows; /* threeD: (row, lane) flags of the pair loop re-examined for uncertain
+                              candidates (each stands for up to four candidates) */
   uint64_t n_queued;       /* threeD: candidates settled by the careful band or the FP64 path;
                               rppi: pairs settled by the box-mode FP32 classifier */
   int weighted;            /* 1: some weight != 1.0 (fixed-point weighted sums) */
