@@ -54,7 +54,7 @@ struct ncorr_batch {
   DevBuf in, cid, pd, pq, pc, count, start, cursor, flags, wmax, bound;
   // Items, histograms, results and the launch's own buffers.
   DevBuf items, hist, out, total, item_off, q_item, q_anchor, s_item, s_anchor, work, stats, xq, xq_count;
-  DevBuf slab_e, slab_m, slab_p, slab_w, slab_q, slab_x, args, args_probe, table, feats;
+  DevBuf slab_e, slab_f, slab_m, slab_p, slab_w, slab_q, slab_x, args, args_probe, table, feats;
   OrderBufs order;
   unsigned xq_cap = 0;
   // Page-locked host mirrors the graph writes.
@@ -331,6 +331,7 @@ int plan(ncorr_batch* b, int autotune) {
     grid_max = std::max(grid_max, c.shp.grid);
   }
   CU(b->slab_e.ensure(slab_n * sizeof(float4)));
+  CU(b->slab_f.ensure(slab_n * sizeof(RowAux)));
   CU(b->slab_m.ensure(slab_n * sizeof(unsigned)));
   CU(b->slab_p.ensure(slab_n * sizeof(int)));
   if (b->weighted) CU(b->slab_w.ensure(slab_n * sizeof(float)));
@@ -351,6 +352,7 @@ int plan(ncorr_batch* b, int autotune) {
   a.work = b->work.as<int>();
   a.flags = b->flags.as<int>() + b->n_cats;
   a.slab_e = b->slab_e.as<float4>();
+  a.slab_f = b->slab_f.as<RowAux>();
   a.slab_m = b->slab_m.as<unsigned>();
   a.slab_p = b->slab_p.as<int>();
   a.slab_w = b->weighted ? b->slab_w.as<float>() : nullptr;
@@ -463,7 +465,7 @@ void ncorr_batch_destroy(ncorr_batch* b) {
   if (b->graph) cudaGraphDestroy(b->graph);
   for (DevBuf* d : {&b->in, &b->cid, &b->pd, &b->pq, &b->pc, &b->count, &b->start, &b->cursor, &b->flags, &b->wmax,
                     &b->bound, &b->items, &b->hist, &b->out, &b->total, &b->item_off, &b->q_item, &b->q_anchor,
-                    &b->s_item, &b->s_anchor, &b->work, &b->stats, &b->xq, &b->xq_count, &b->slab_e, &b->slab_m,
+                    &b->s_item, &b->s_anchor, &b->work, &b->stats, &b->xq, &b->xq_count, &b->slab_e, &b->slab_f, &b->slab_m,
                     &b->slab_p, &b->slab_w, &b->slab_q, &b->slab_x, &b->args, &b->args_probe, &b->table, &b->feats})
     d->release();
   b->order.release();

@@ -35,6 +35,14 @@ constexpr unsigned kCodeCareful = 0xFFu;
 // careful candidates add into (the bin table's codes for them), so the
 // candidate bodies need not test the code. Nothing reads the sinks.
 __host__ __device__ inline int hist_row(int nb) { return nb + 2; }
+
+// Per neighbour-list entry, next to its offset and rho^2 (a float4): the
+// values the pair loop needs when the entry is a row, computed once when the
+// list is built: 2 rho, and bin * (the histogram stride of bin_j).
+struct __align__(8) RowAux {
+  float a2r;
+  unsigned key;
+};
 __host__ __device__ inline int hist_words(int nb) { return nb * nb * hist_row(nb); }
 // Bin-table codes of "reject" and "careful": with a CTA histogram (code
 // scale = the byte stride of a bin, > 1) the two sink bins of the row; with

@@ -66,11 +66,16 @@ constexpr unsigned kSinceDrainBits = 20;  // 2^20 units = 2^30 candidates
 // Upper bound of the waits for the histogram slot (iterations of ~0.5 us).
 constexpr int kSlotSpinLimit = 1 << 22;
 
+// Ring of points that passed the prefilter of the list build, per warp.
+constexpr unsigned kRing = 64;
+
 // Per-warp slot table of the anchor being listed (shared memory).
 struct SlotTab {
   double shift[27][3];  // image shift of the slot (0 or +-box per axis)
   float dof[27][3];     // FP32 offset of the slot's cell origin from the home cell's
   int start2[27], pre2[28], start3[27], pre3[28];
+  int ring_j[kRing];              // pending points: index in the catalogue
+  unsigned char ring_s[kRing];    // and slot
 };
 
 // Shared-memory layout (dynamic part). The bin table sits at offset 0 and the
@@ -118,8 +123,11 @@ struct KArgs {
   int* work;
   int* flags;
   // Per-warp global slabs: neighbour lists (kcap2 entries for p2, then kcap3
-  // for p3; kcap3 = 0 when p2 == p3), careful queue, exact buffer.
+  // for p3; kcap3 = 0 when p2 == p3; one entry past a list holds the padding
+  // row), careful queue, exact buffer. A list entry: offset d and rho^2 (e),
+  // 2 rho and row key (f), bin and slot (m), point (p), weight (w).
   float4* slab_e;
+  RowAux* slab_f;
   unsigned* slab_m;
   int* slab_p;
   float* slab_w;
@@ -174,14 +182,16 @@ __device__ __forceinline__ unsigned careful_code(float v, const float* e2lo, con
 // A neighbour list in global memory.
 struct ListView {
   float4* e;
+  RowAux* f;
   unsigned* m;
   int* p;
   float* w;
 };
 
 // The margin form of the triangle test. List entries keep rho = sqrt_rn of
-// their r^2 estimate in .w; with a = rho_j^2 and b = rho_l^2 (the products
-// formed inside the FMAs) a candidate of third side v is certainly kept by
+// their r^2 estimate (as rho^2 = fmul_rn(rho, rho) and 2 rho); with
+// a = rho_j^2 and b = rho_l^2 (the product formed inside the FMA) a candidate
+// of third side v is certainly kept by
 // the reference's FP32 sqrtf test when |v - (a + b)| < 2 rho_j rho_l - M
 // (hm = -M; the PTX bodies evaluate the same operations).
 __device__ __forceinline__ bool heron_clean(float v, float aj, float a2r, float rl, float hm) {
@@ -594,6 +604,8 @@ __device__ __noinline__ void cold_drain(Cold& c, int lb, int k3, int qn) {
         }
         const float4 ej = c.l2.e[j];
         const float4 el = c.l3.e[min(l, k3 - 1)];
+        const float a2rj = c.l2.f[j].a2r;
+        const float rhol = 0.5f * c.l3.f[min(l, k3 - 1)].a2r;
         // A row's bit stands for all its column slots: keep the candidates
         // the body itself flagged (its classification, recomputed with the
         // same operations), not the ones it counted or rejected.
@@ -603,10 +615,10 @@ __device__ __noinline__ void cold_drain(Cold& c, int lb, int k3, int qn) {
           r.x = ej.x;
           r.y = ej.y;
           r.z = ej.z;
-          r.a = __fmul_rn(ej.w, ej.w);
-          r.a2r = 2.0f * ej.w;
+          r.a = ej.w;
+          r.a2r = a2rj;
           r.key = 0;
-          const float4 lc = make_float4(-2.0f * el.x, -2.0f * el.y, -2.0f * el.z, el.w);
+          const float4 lc = make_float4(-2.0f * el.x, -2.0f * el.y, -2.0f * el.z, rhol);
           unsigned bc;
           bool clean;
           cand_classify(r, lc, c.tab, g.tab_scale, g.tab_n, g.hm, &bc, &clean);
@@ -621,7 +633,7 @@ __device__ __noinline__ void cold_drain(Cold& c, int lb, int k3, int qn) {
           const float v = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
           unsigned code = careful_code(v, c.e2lo, c.e2hi, nb, g.ka, g.kb);
           if (code < static_cast<unsigned>(nb)) {
-            if (!heron_clean(v, __fmul_rn(ej.w, ej.w), 2.0f * ej.w, el.w, g.hm)) code = kCodeExact;
+            if (!heron_clean(v, ej.w, a2rj, rhol, g.hm)) code = kCodeExact;
           }
           if (code == kCodeExact) {
             ++c.n_exact_tri;
@@ -752,12 +764,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_triangles(KArgs a) {
     const size_t stride = static_cast<size_t>(a.kcap2) + a.kcap3;
     const size_t b2 = gw * stride, b3 = b2 + a.kcap2;
     l2.e = a.slab_e + b2;
+    l2.f = a.slab_f + b2;
     l2.m = a.slab_m + b2;
     l2.p = a.slab_p + b2;
     l2.w = a.slab_w ? a.slab_w + b2 : nullptr;
     l3 = l2;
     if (!SYM) {
       l3.e = a.slab_e + b3;
+      l3.f = a.slab_f + b3;
       l3.m = a.slab_m + b3;
       l3.p = a.slab_p + b3;
       l3.w = a.slab_w ? a.slab_w + b3 : nullptr;
@@ -956,66 +970,59 @@ __global__ void __launch_bounds__(kThreads, 1) k_triangles(KArgs a) {
       __syncwarp();
     }
 
-    // ---- Phase A: neighbour lists (in global memory, this warp's slab)
+    // ---- Phase A: neighbour lists (in global memory, this warp's slab). A
+    // list holds at most cap - 1 entries; the entry after its last one is
+    // the padding row. The slots' points stream past in rounds of 32 (each
+    // round's cell-local FP32 points loaded two rounds ahead); a prefilter
+    // drops those certainly out of range and puts the others in the warp's
+    // ring of pending points. Whenever 32 are pending they are settled one
+    // per lane: 32 independent FP64 position loads in flight at once, then
+    // the exact offset, its classification and the append to the list.
     auto build = [&](const Catalog& cat, const int* pre, const int* stt, ListView& lv, int cap) -> int {
       const int total = pre[27];
       const int rounded = (total + 31) & ~31;
       int cnt = 0;
-      // Software pipeline: the next round's point is loaded before this
-      // round's is classified, so two loads are in flight per thread.
-      int sn = 0, jn = 0;
-      float4 qn = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-      if (lane < total) {
-        while (lane >= pre[sn + 1]) ++sn;
-        jn = stt[sn] + (lane - pre[sn]);
-        qn = cat.pq[jn];
-      }
-      for (int base = 0; base < rounded; base += 32) {
-        const int item_i = base + lane;
-        const int s = sn, j = jn;
-        const float4 q = qn;
-        const int next = item_i + 32;
-        if (next < total) {
-          while (next >= pre[sn + 1]) ++sn;
-          jn = stt[sn] + (next - pre[sn]);
-          qn = cat.pq[jn];
-        }
+      cap -= 1;
+      unsigned head = 0, pend = 0;  // ring position of the oldest pending point; pending points
+      auto settle = [&](int n) {
+        __syncwarp();  // the ring entries written by all lanes are visible
         bool acc = false;
         float4 ent;
+        RowAux aux;
         unsigned meta = 0;
         float wv = 0.0f;
-        if (item_i < total) {
-          // Cell-local FP32 prefilter: skip candidates certainly out of range.
-          const float fx = (q.x - qa.x) + st.dof[s][0];
-          const float fy = (q.y - qa.y) + st.dof[s][1];
-          const float fz = (q.z - qa.z) + st.dof[s][2];
-          const float vp = fmaf(fz, fz, fmaf(fy, fy, fx * fx));
-          if (vp < g.pre_hi && vp > g.pre_lo && (!sym6 || j > ai)) {
-            // Exact anchor-relative offset of the image (FP64), rounded once.
-            const double4_16a p = cat.pd[j];
-            const double px = __dadd_rn(p.x, st.shift[s][0]);
-            const double py = __dadd_rn(p.y, st.shift[s][1]);
-            const double pz = __dadd_rn(p.z, st.shift[s][2]);
-            const float dx = __double2float_rn(__dsub_rn(px, pa.x));
-            const float dy = __double2float_rn(__dsub_rn(py, pa.y));
-            const float dz = __double2float_rn(__dsub_rn(pz, pa.z));
-            const float v = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-            unsigned code = table_code(v, tab, g.tab_scale, g.tab_n);
-            if (code < nb_cs) {
-              code /= cs;
-            } else if (code == car) {
-              code = careful_code(v, s_e2lo, s_e2hi, nb, g.ka, g.kb);
-            }
-            if (code == kCodeExact) {
-              ++c.n_exact_pair;
-              code = cold_pair_exact(&a.self->g, s_sqr_bins, pa, px, py, pz);
-            }
-            if (code < static_cast<unsigned>(nb)) {
-              acc = true;
-              ent = make_float4(dx, dy, dz, __fsqrt_rn(v));
-              meta = code | (static_cast<unsigned>(s) << 8);
-              wv = q.w;
-            }
+        int j = 0;
+        if (lane < n) {
+          const unsigned slot_i = (head + static_cast<unsigned>(lane)) & (kRing - 1);
+          j = st.ring_j[slot_i];
+          const int s = st.ring_s[slot_i];
+          // Exact anchor-relative offset of the image (FP64), rounded once.
+          const double4_16a p = cat.pd[j];
+          const double px = __dadd_rn(p.x, st.shift[s][0]);
+          const double py = __dadd_rn(p.y, st.shift[s][1]);
+          const double pz = __dadd_rn(p.z, st.shift[s][2]);
+          const float dx = __double2float_rn(__dsub_rn(px, pa.x));
+          const float dy = __double2float_rn(__dsub_rn(py, pa.y));
+          const float dz = __double2float_rn(__dsub_rn(pz, pa.z));
+          const float v = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+          unsigned code = table_code(v, tab, g.tab_scale, g.tab_n);
+          if (code < nb_cs) {
+            code /= cs;
+          } else if (code == car) {
+            code = careful_code(v, s_e2lo, s_e2hi, nb, g.ka, g.kb);
+          }
+          if (code == kCodeExact) {
+            ++c.n_exact_pair;
+            code = cold_pair_exact(&a.self->g, s_sqr_bins, pa, px, py, pz);
+          }
+          if (code < static_cast<unsigned>(nb)) {
+            acc = true;
+            const float rho = __fsqrt_rn(v);
+            ent = make_float4(dx, dy, dz, __fmul_rn(rho, rho));
+            aux.a2r = 2.0f * rho;
+            aux.key = code * kj_mul;
+            meta = code | (static_cast<unsigned>(s) << 8);
+            wv = __double2float_rn(p.w);
           }
         }
         const unsigned bal = __ballot_sync(FULL, acc);
@@ -1023,6 +1030,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_triangles(KArgs a) {
           const int e = cnt + __popc(bal & lt_mask);
           if (e < cap) {
             lv.e[e] = ent;
+            lv.f[e] = aux;
             lv.m[e] = meta;
             lv.p[e] = j;
             if (WEIGHTED) lv.w[e] = wv;
@@ -1031,11 +1039,65 @@ __global__ void __launch_bounds__(kThreads, 1) k_triangles(KArgs a) {
           }
         }
         cnt += __popc(bal);
+        head += static_cast<unsigned>(n);
+        pend -= static_cast<unsigned>(n);
+        __syncwarp();  // the ring entries are read before the next round overwrites them
+      };
+      // Round r's point (slot, index, FP32 values) of this lane, rounds r
+      // and r + 1 in flight.
+      int sn = 0;
+      auto fetch = [&](int item, int& s, int& j, float4& q) {
+        if (item < total) {
+          while (item >= pre[sn + 1]) ++sn;
+          s = sn;
+          j = stt[sn] + (item - pre[sn]);
+          q = cat.pq[j];
+        }
+      };
+      int s0 = 0, j0 = 0, s1 = 0, j1 = 0;
+      float4 q0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), q1 = q0;
+      fetch(lane, s0, j0, q0);
+      fetch(lane + 32, s1, j1, q1);
+      for (int base = 0; base < rounded; base += 32) {
+        const int item_i = base + lane;
+        const int s = s0, j = j0;
+        const float4 q = q0;
+        s0 = s1;
+        j0 = j1;
+        q0 = q1;
+        fetch(item_i + 64, s1, j1, q1);
+        bool pass = false;
+        if (item_i < total) {
+          // Cell-local FP32 prefilter: skip candidates certainly out of range.
+          const float fx = (q.x - qa.x) + st.dof[s][0];
+          const float fy = (q.y - qa.y) + st.dof[s][1];
+          const float fz = (q.z - qa.z) + st.dof[s][2];
+          const float vp = fmaf(fz, fz, fmaf(fy, fy, fx * fx));
+          pass = vp < g.pre_hi && vp > g.pre_lo && (!sym6 || j > ai);
+        }
+        const unsigned bal = __ballot_sync(FULL, pass);
+        if (pass) {
+          const unsigned slot_i = (head + pend + static_cast<unsigned>(__popc(bal & lt_mask))) & (kRing - 1);
+          st.ring_j[slot_i] = j;
+          st.ring_s[slot_i] = static_cast<unsigned char>(s);
+        }
+        pend += static_cast<unsigned>(__popc(bal));
+        if (pend >= 32u) settle(32);
       }
+      if (pend > 0u) settle(static_cast<int>(pend));
       return min(cnt, cap);
     };
     const int k2 = build(it.c2, st.pre2, st.start2, l2, a.kcap2);
     const int k3 = SYM ? k2 : build(it.c3, st.pre3, st.start3, l3, a.kcap3);
+    if (lane == 0) {
+      // The padding row after the rows: rho = 1e18 gives v >= 1e36 against
+      // every column, rejected by the table, with a margin test that holds;
+      // so it adds into sink bins and is never flagged. Row loops that run
+      // past their last row read it instead of testing for the end.
+      l2.e[k2] = make_float4(0.0f, 0.0f, 0.0f, 1.0e36f);
+      l2.f[k2] = RowAux{2.0e18f, 0u};
+      if (WEIGHTED) l2.w[k2] = 0.0f;
+    }
     __syncwarp();  // the lists written by all lanes are visible to all lanes
     {
       const unsigned long long pairs_here = SYM ? static_cast<unsigned long long>(k2) * (k2 > 0 ? k2 - 1 : 0) / 2
@@ -1071,8 +1133,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_triangles(KArgs a) {
         if (!HG && (old >> kSinceDrainBits) != ((old + units) >> kSinceDrainBits))
           drain_hist<WEIGHTED>(a.self, hist_s, nb, copies, held, lane, 32);
       }
-      // Columns are held as (-2 d_l, rho_l); the padding (0, rho = 1e18)
-      // gives v = 1e36 and is rejected by the table for every row.
+      // Columns are held as (-2 d_l, rho_l) with the lane's histogram base in
+      // their key; the padding (0, rho = 1e18) gives v = 1e36 and is
+      // rejected by the table for every row.
+      const unsigned col_base = HG ? 0u : hist_sh;
       ColV col;
       float wl[kReg];
 #pragma unroll
@@ -1080,23 +1144,23 @@ __global__ void __launch_bounds__(kThreads, 1) k_triangles(KArgs a) {
         const int l = lb + r * 32 + lane;
         if (l < k3) {
           const float4 e = l3.e[l];
-          col.l[r] = make_float4(-2.0f * e.x, -2.0f * e.y, -2.0f * e.z, e.w);
-          col.k[r] = (l3.m[l] & 0xffu) * kl_mul;
+          col.l[r] = make_float4(-2.0f * e.x, -2.0f * e.y, -2.0f * e.z, 0.5f * l3.f[l].a2r);
+          col.k[r] = (l3.m[l] & 0xffu) * kl_mul + col_base;
           wl[r] = WEIGHTED ? l3.w[l] : 0.0f;
         } else {
           col.l[r] = make_float4(0.0f, 0.0f, 0.0f, 1.0e18f);
-          col.k[r] = 0;
+          col.k[r] = col_base;
           wl[r] = 0.0f;
         }
       }
-      auto make_row = [&](float4 e, unsigned m) {
+      auto make_row = [&](const float4& e, const RowAux& f) {
         RowV r;
         r.x = e.x;
         r.y = e.y;
         r.z = e.z;
-        r.a = __fmul_rn(e.w, e.w);
-        r.a2r = 2.0f * e.w;
-        r.key = HG ? (m & 0xffu) * kj_mul : (m & 0xffu) * kj_mul + hist_sh;
+        r.a = e.w;
+        r.a2r = f.a2r;
+        r.key = f.key;
         return r;
       };
       // The careful queue: entries of this tile, settled when it fills and
@@ -1127,19 +1191,46 @@ __global__ void __launch_bounds__(kThreads, 1) k_triangles(KArgs a) {
           cand_wsum(r, cl, ck, in, bk, wa * wj * wsc, cw, rbit, q);
         }
       };
-      // Rows [jb, je) of one flag group against column slots 0..N-1.
+      // One row against column slots 0..N-1.
+      auto row_at = [&](const float4& e, const RowAux& f, float wj, unsigned rbit, auto n_tag, unsigned& q) {
+        constexpr int N = decltype(n_tag)::value;
+        const RowV r = make_row(e, f);
+        if (WEIGHTED || HG) {
+#pragma unroll
+          for (int s = 0; s < N; ++s) cand_slow(r, col.l[s], col.k[s], wl[s], 1u, wj, rbit, q);
+        } else {
+          row_full<N>(r, col, bk, rbit, q);
+        }
+      };
+      // Rows [jb, je) of one flag group against column slots 0..N-1, R rows
+      // per iteration; a row position at or past je reads the padding row
+      // (index k2), which only adds into sinks, so the loop has no remainder
+      // test. The bodies' "memory" clobber keeps the compiler from hoisting
+      // loads above a body, so each row's registers are reloaded with the row
+      // R positions ahead right after its body: the load has the next R - 1
+      // bodies' time to land, and no register is copied.
       auto rows = [&](int jb, int je, auto n_tag, unsigned& q) {
         constexpr int N = decltype(n_tag)::value;
-#pragma unroll(N == kReg ? 2 : 1)
-        for (int j = jb; j < je; ++j) {
-          const RowV r = make_row(l2.e[j], l2.m[j]);
-          const unsigned rbit = 1u << (j - jb);
-          if (WEIGHTED || HG) {
-            const float wj = WEIGHTED ? l2.w[j] : 0.0f;
+        constexpr int R = N == kReg ? 4 : 2;
+        float4 e[R];
+        RowAux f[R];
+        float w[R];
 #pragma unroll
-            for (int s = 0; s < N; ++s) cand_slow(r, col.l[s], col.k[s], wl[s], 1u, wj, rbit, q);
-          } else {
-            row_full<N>(r, col, bk, rbit, q);
+        for (int p = 0; p < R; ++p) {
+          const int jj = jb + p < je ? jb + p : k2;
+          e[p] = l2.e[jj];
+          f[p] = l2.f[jj];
+          w[p] = WEIGHTED ? l2.w[jj] : 0.0f;
+        }
+#pragma unroll 1
+        for (int j = jb; j < je; j += R) {
+#pragma unroll
+          for (int p = 0; p < R; ++p) {
+            row_at(e[p], f[p], w[p], 1u << ((j + p - jb) & 31), n_tag, q);
+            const int jj = j + R + p < je ? j + R + p : k2;
+            e[p] = l2.e[jj];
+            f[p] = l2.f[jj];
+            w[p] = WEIGHTED ? l2.w[jj] : 0.0f;
           }
         }
       };
@@ -1183,17 +1274,40 @@ __global__ void __launch_bounds__(kThreads, 1) k_triangles(KArgs a) {
           }
           const bool cval = bb + lane < k2;
           unsigned qd = 0;
-#pragma unroll 2
-          for (int d = 1; d <= 16; ++d) {
+          // Each lane's rows of steps d and d + 1 are in flight; a row
+          // position past the list reads the padding row (masked anyway).
+          auto rot_row = [&](int d) {
             const int rr = bb + ((lane + d) & 31);
-            const unsigned in = (cval && rr < k2 && (d < 16 || lane < 16)) ? 1u : 0u;
-            const int rl = min(rr, k2 - 1);
-            const RowV r = make_row(l2.e[rl], l2.m[rl]);
-            const unsigned rbit = 1u << (d - 1);
-            if (WEIGHTED || HG)
-              cand_slow(r, cl, ck, cw, in, WEIGHTED ? l2.w[rl] : 0.0f, rbit, qd);
-            else
-              row_rot1(r, cl, ck, bk, rbit, in, qd);
+            return rr < k2 ? rr : k2;
+          };
+          float4 re[2];
+          RowAux rf[2];
+          float rw[2];
+#pragma unroll
+          for (int p = 0; p < 2; ++p) {
+            const int jj = rot_row(1 + p);
+            re[p] = l2.e[jj];
+            rf[p] = l2.f[jj];
+            rw[p] = WEIGHTED ? l2.w[jj] : 0.0f;
+          }
+#pragma unroll 1
+          for (int d0 = 1; d0 <= 16; d0 += 2) {
+#pragma unroll
+            for (int p = 0; p < 2; ++p) {
+              const int d = d0 + p;
+              const int rr = bb + ((lane + d) & 31);
+              const unsigned in = (cval && rr < k2 && (d < 16 || lane < 16)) ? 1u : 0u;
+              const RowV r = make_row(re[p], rf[p]);
+              const unsigned rbit = 1u << (d - 1);
+              if (WEIGHTED || HG)
+                cand_slow(r, cl, ck, cw, in, rw[p], rbit, qd);
+              else
+                row_rot1(r, cl, ck, bk, rbit, in, qd);
+              const int jj = rot_row(d + 2);
+              re[p] = l2.e[jj];
+              rf[p] = l2.f[jj];
+              rw[p] = WEIGHTED ? l2.w[jj] : 0.0f;
+            }
           }
           enqueue(qd, (static_cast<unsigned>(bb) << 8) | (kKindRot << 5) | static_cast<unsigned>(lane));
         }
