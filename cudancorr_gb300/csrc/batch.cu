@@ -54,7 +54,7 @@ struct ncorr_batch {
   DevBuf in, cid, pd, pq, pc, count, start, cursor, flags, wmax, bound;
   // Items, histograms, results and the launch's own buffers.
   DevBuf items, hist, out, total, item_off, q_item, q_anchor, s_item, s_anchor, work, stats, xq, xq_count;
-  DevBuf slab_e, slab_f, slab_m, slab_p, slab_w, slab_q, slab_x, args, args_probe, table, feats;
+  DevBuf slab_e, slab_w, slab_q, slab_x, args, args_probe, table, feats;
   OrderBufs order;
   unsigned xq_cap = 0;
   // Page-locked host mirrors the graph writes.
@@ -330,10 +330,7 @@ int plan(ncorr_batch* b, int autotune) {
     slab_n = std::max(slab_n, tri_slab_entries(c.shp));
     grid_max = std::max(grid_max, c.shp.grid);
   }
-  CU(b->slab_e.ensure(slab_n * sizeof(float4)));
-  CU(b->slab_f.ensure(slab_n * sizeof(RowAux)));
-  CU(b->slab_m.ensure(slab_n * sizeof(unsigned)));
-  CU(b->slab_p.ensure(slab_n * sizeof(int)));
+  CU(b->slab_e.ensure(slab_n * sizeof(ListEnt)));
   if (b->weighted) CU(b->slab_w.ensure(slab_n * sizeof(float)));
   CU(b->slab_q.ensure(static_cast<size_t>(grid_max) * kWarps * kQueueCap * sizeof(unsigned long long)));
   CU(b->slab_x.ensure(static_cast<size_t>(grid_max) * kWarps * 32 * sizeof(ExactEntry)));
@@ -351,10 +348,7 @@ int plan(ncorr_batch* b, int autotune) {
   a.table = b->table.as<unsigned char>();
   a.work = b->work.as<int>();
   a.flags = b->flags.as<int>() + b->n_cats;
-  a.slab_e = b->slab_e.as<float4>();
-  a.slab_f = b->slab_f.as<RowAux>();
-  a.slab_m = b->slab_m.as<unsigned>();
-  a.slab_p = b->slab_p.as<int>();
+  a.slab_e = b->slab_e.as<ListEnt>();
   a.slab_w = b->weighted ? b->slab_w.as<float>() : nullptr;
   a.slab_q = b->slab_q.as<unsigned long long>();
   a.slab_x = b->slab_x.as<ExactEntry>();
@@ -465,8 +459,8 @@ void ncorr_batch_destroy(ncorr_batch* b) {
   if (b->graph) cudaGraphDestroy(b->graph);
   for (DevBuf* d : {&b->in, &b->cid, &b->pd, &b->pq, &b->pc, &b->count, &b->start, &b->cursor, &b->flags, &b->wmax,
                     &b->bound, &b->items, &b->hist, &b->out, &b->total, &b->item_off, &b->q_item, &b->q_anchor,
-                    &b->s_item, &b->s_anchor, &b->work, &b->stats, &b->xq, &b->xq_count, &b->slab_e, &b->slab_f, &b->slab_m,
-                    &b->slab_p, &b->slab_w, &b->slab_q, &b->slab_x, &b->args, &b->args_probe, &b->table, &b->feats})
+                    &b->s_item, &b->s_anchor, &b->work, &b->stats, &b->xq, &b->xq_count, &b->slab_e,
+                    &b->slab_w, &b->slab_q, &b->slab_x, &b->args, &b->args_probe, &b->table, &b->feats})
     d->release();
   b->order.release();
   for (double* p : {b->h_out})

@@ -135,10 +135,7 @@ int run(ncorr_handle* h, const double4_16a* d1, int n1, const double4_16a* d2, i
     return fail(NCORR_ERR_CUDA, "triangle kernel does not fit on the device, or a 27-cell neighbourhood holds "
                                 "more than 2^24 points");
   const size_t slab_n = tri_slab_entries(shp);
-  CU(h->slab_e.ensure(slab_n * sizeof(float4)));
-  CU(h->slab_f.ensure(slab_n * sizeof(RowAux)));
-  CU(h->slab_m.ensure(slab_n * sizeof(unsigned)));
-  CU(h->slab_p.ensure(slab_n * sizeof(int)));
+  CU(h->slab_e.ensure(slab_n * sizeof(ListEnt)));
   if (weighted) CU(h->slab_w.ensure(slab_n * sizeof(float)));
   CU(h->slab_q.ensure(static_cast<size_t>(shp.grid) * kWarps * kQueueCap * sizeof(unsigned long long)));
   CU(h->slab_x.ensure(static_cast<size_t>(shp.grid) * kWarps * 32 * sizeof(ExactEntry)));
@@ -204,10 +201,7 @@ int run(ncorr_handle* h, const double4_16a* d1, int n1, const double4_16a* d2, i
   a.table = h->d_table.as<unsigned char>();
   a.work = h->d_work.as<int>();
   a.flags = h->d_flags.as<int>() + 4;
-  a.slab_e = h->slab_e.as<float4>();
-  a.slab_f = h->slab_f.as<RowAux>();
-  a.slab_m = h->slab_m.as<unsigned>();
-  a.slab_p = h->slab_p.as<int>();
+  a.slab_e = h->slab_e.as<ListEnt>();
   a.slab_w = weighted ? h->slab_w.as<float>() : nullptr;
   a.slab_q = h->slab_q.as<unsigned long long>();
   a.slab_x = h->slab_x.as<ExactEntry>();
@@ -458,7 +452,7 @@ void ncorr_destroy(ncorr_handle* h) {
     c.pc.release();
   }
   for (DevBuf* b : {&h->d_table, &h->d_flags, &h->d_wmax, &h->d_work, &h->d_bound, &h->d_hist,
-                    &h->d_out, &h->d_stats, &h->d_total, &h->slab_e, &h->slab_f, &h->slab_m, &h->slab_p,
+                    &h->d_out, &h->d_stats, &h->d_total, &h->slab_e,
                     &h->slab_w, &h->slab_q, &h->slab_x, &h->cta_time, &h->xq, &h->xq_count, &h->d_args, &h->d_items, &h->d_cell_work,
                     &h->d_feats, &h->q_item, &h->q_anchor, &h->rp_pos, &h->rp_ab, &h->rp_rel, &h->rp_meta})
     b->release();
@@ -1011,20 +1005,16 @@ static int count_noalloc_impl(const double box[3], const double* edges, int n_ed
     return fail(NCORR_ERR_CUDA, "triangle kernel does not fit on the device, or a 27-cell neighbourhood holds "
                                 "more than 2^24 points");
   const size_t per_warp_entries = static_cast<size_t>(shp.kcap2) + shp.kcap3;
-  const size_t per_cta = kWarps * (per_warp_entries * (sizeof(float4) + sizeof(RowAux) + sizeof(unsigned) +
-                                                       sizeof(int) + sizeof(float)) +
+  const size_t per_cta = kWarps * (per_warp_entries * (sizeof(ListEnt) + sizeof(float)) +
                                    kQueueCap * sizeof(unsigned long long) + 32 * sizeof(ExactEntry));
-  // Seven 256-byte roundings of the slab arrays, at most.
-  const size_t usable = slab_bytes > 7 * 256 ? slab_bytes - 7 * 256 : 0;
+  // Four 256-byte roundings of the slab arrays, at most.
+  const size_t usable = slab_bytes > 4 * 256 ? slab_bytes - 4 * 256 : 0;
   const int fit = static_cast<int>(std::min<size_t>(usable / per_cta, static_cast<size_t>(shp.grid)));
   if (fit < 1)
     return fail(NCORR_ERR_CAPACITY, "ncorr_count_noalloc: neighbourhoods too dense for its fixed scratch");
   shp.grid = fit;
   const size_t slab_n = tri_slab_entries(shp);
-  float4* slab_e = reinterpret_cast<float4*>(take(slab_n * sizeof(float4)));
-  RowAux* slab_f = reinterpret_cast<RowAux*>(take(slab_n * sizeof(RowAux)));
-  unsigned* slab_m = reinterpret_cast<unsigned*>(take(slab_n * sizeof(unsigned)));
-  int* slab_p = reinterpret_cast<int*>(take(slab_n * sizeof(int)));
+  ListEnt* slab_e = reinterpret_cast<ListEnt*>(take(slab_n * sizeof(ListEnt)));
   float* slab_w = reinterpret_cast<float*>(take(slab_n * sizeof(float)));
   unsigned long long* slab_q = reinterpret_cast<unsigned long long*>(
       take(static_cast<size_t>(shp.grid) * kWarps * kQueueCap * sizeof(unsigned long long)));
@@ -1074,9 +1064,6 @@ static int count_noalloc_impl(const double box[3], const double* edges, int n_ed
   a.work = work;
   a.flags = flags + 4;
   a.slab_e = slab_e;
-  a.slab_f = slab_f;
-  a.slab_m = slab_m;
-  a.slab_p = slab_p;
   a.slab_w = weighted ? slab_w : nullptr;
   a.slab_q = slab_q;
   a.slab_x = slab_x;

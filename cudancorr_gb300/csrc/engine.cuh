@@ -36,13 +36,21 @@ constexpr unsigned kCodeCareful = 0xFFu;
 // candidate bodies need not test the code. Nothing reads the sinks.
 __host__ __device__ inline int hist_row(int nb) { return nb + 2; }
 
-// Per neighbour-list entry, next to its offset and rho^2 (a float4): the
-// values the pair loop needs when the entry is a row, computed once when the
-// list is built: 2 rho, and bin * (the histogram stride of bin_j).
-struct __align__(8) RowAux {
+// One neighbour-list entry of the triangle kernel (32 bytes): the offset d
+// from the anchor and rho^2 (rho = sqrt_rn of the r1^2 estimate), then what
+// the pair loop needs when the entry is a row, computed once when the list is
+// built: 2 rho and bin * (the histogram stride of bin_j); then bin | slot << 8
+// and the point's index in its catalogue.
+struct __align__(16) ListEnt {
+  float4 e;
   float a2r;
   unsigned key;
+  unsigned m;
+  int p;
 };
+// Padding records after each list: a row loop that runs up to this many rows
+// past the list's end reads padding rows, which add into sink bins only.
+constexpr int kListPad = 8;
 __host__ __device__ inline int hist_words(int nb) { return nb * nb * hist_row(nb); }
 // Bin-table codes of "reject" and "careful": with a CTA histogram (code
 // scale = the byte stride of a bin, > 1) the two sink bins of the row; with

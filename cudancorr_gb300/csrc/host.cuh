@@ -152,7 +152,7 @@ struct ncorr_handle {
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   ncorr_host::CatDev cat[3];
   ncorr_host::DevBuf d_table, d_flags, d_wmax, d_work, d_bound, d_hist, d_out, d_stats, d_total;
-  ncorr_host::DevBuf slab_e, slab_f, slab_m, slab_p, slab_w, slab_q, slab_x, cta_time;
+  ncorr_host::DevBuf slab_e, slab_w, slab_q, slab_x, cta_time;
   ncorr_host::DevBuf xq, xq_count;  // deferred exact candidates
   ncorr_host::DevBuf d_args;        // global copy of the triangle kernel's arguments
   unsigned xq_cap = 0;
@@ -315,9 +315,9 @@ inline bool tri_shape(int nb, bool survey, bool sym, bool weighted, bool hg, int
   out->smem = static_cast<size_t>(L.total);
   const int64_t ctas_needed = std::max<int64_t>(1, (n_work + kWarps - 1) / kWarps);
   out->grid = static_cast<int>(std::min<int64_t>(static_cast<int64_t>(nsm) * occ, ctas_needed));
-  // One entry more than the largest list: the padding row after it.
-  out->kcap2 = ((std::max(bound2, 1) + 1 + 31) / 32) * 32;
-  out->kcap3 = sym ? 0 : ((std::max(bound3, 1) + 1 + 31) / 32) * 32;
+  // kListPad entries more than the largest list: the padding rows after it.
+  out->kcap2 = ((std::max(bound2, 1) + kListPad + 31) / 32) * 32;
+  out->kcap3 = sym ? 0 : ((std::max(bound3, 1) + kListPad + 31) / 32) * 32;
   // The careful queue names list rows in 24 bits.
   return out->kcap2 <= kListMax && out->kcap3 <= kListMax;
 }

@@ -123,13 +123,9 @@ struct KArgs {
   int* work;
   int* flags;
   // Per-warp global slabs: neighbour lists (kcap2 entries for p2, then kcap3
-  // for p3; kcap3 = 0 when p2 == p3; one entry past a list holds the padding
-  // row), careful queue, exact buffer. A list entry: offset d and rho^2 (e),
-  // 2 rho and row key (f), bin and slot (m), point (p), weight (w).
-  float4* slab_e;
-  RowAux* slab_f;
-  unsigned* slab_m;
-  int* slab_p;
+  // for p3; kcap3 = 0 when p2 == p3; the kListPad entries past a list hold
+  // padding rows) with their weights, careful queue, exact buffer.
+  ListEnt* slab_e;
   float* slab_w;
   unsigned long long* slab_q;
   ExactEntry* slab_x;
@@ -181,10 +177,7 @@ __device__ __forceinline__ unsigned careful_code(float v, const float* e2lo, con
 
 // A neighbour list in global memory.
 struct ListView {
-  float4* e;
-  RowAux* f;
-  unsigned* m;
-  int* p;
+  ListEnt* v;
   float* w;
 };
 
@@ -346,6 +339,17 @@ __device__ __forceinline__ void row_rot1(const RowV& r, const float4& l, unsigne
                : "f"(r.x), "f"(r.y), "f"(r.z), "f"(r.a), "f"(r.a2r), "r"(r.key), "f"(k.tscale), "r"(k.tab_adj),
                  "r"(k.tab_last), "r"(k.car), "f"(k.hm), "r"(k.dummy), "r"(rbit), "f"(l.x), "f"(l.y), "f"(l.z),
                  "f"(l.w), "r"(kl), "r"(mask)
+               : "memory");
+}
+
+// The same without a mask (a full diagonal block, d < 16).
+__device__ __forceinline__ void row_rot1_full(const RowV& r, const float4& l, unsigned kl, const BodyK& k,
+                                              unsigned rbit, unsigned& q) {
+  asm volatile("{\n\t" NCORR_DECL(0) NCORR_CLSX(0, NCORR_C0) NCORR_UPD(0, "%17", "%18") NCORR_FLAG NCORR_RED(0) "}"
+               : "+r"(q)
+               : "f"(r.x), "f"(r.y), "f"(r.z), "f"(r.a), "f"(r.a2r), "r"(r.key), "f"(k.tscale), "r"(k.tab_adj),
+                 "r"(k.tab_last), "r"(k.car), "f"(k.hm), "r"(k.dummy), "r"(rbit), "f"(l.x), "f"(l.y), "f"(l.z),
+                 "f"(l.w), "r"(kl)
                : "memory");
 }
 
@@ -602,10 +606,11 @@ __device__ __noinline__ void cold_drain(Cold& c, int lb, int k3, int qn) {
           s = 0;
           bits &= bits - 1u;
         }
-        const float4 ej = c.l2.e[j];
-        const float4 el = c.l3.e[min(l, k3 - 1)];
-        const float a2rj = c.l2.f[j].a2r;
-        const float rhol = 0.5f * c.l3.f[min(l, k3 - 1)].a2r;
+        const ListEnt& ejv = c.l2.v[j];
+        const ListEnt& elv = c.l3.v[min(l, k3 - 1)];
+        const float4 ej = ejv.e, el = elv.e;
+        const float a2rj = ejv.a2r;
+        const float rhol = 0.5f * elv.a2r;
         // A row's bit stands for all its column slots: keep the candidates
         // the body itself flagged (its classification, recomputed with the
         // same operations), not the ones it counted or rejected.
@@ -627,8 +632,8 @@ __device__ __noinline__ void cold_drain(Cold& c, int lb, int k3, int qn) {
         }
         if (flagged) {
           ++c.n_queued;
-          const unsigned mj = c.l2.m[j];
-          const unsigned ml = c.l3.m[l];
+          const unsigned mj = ejv.m;
+          const unsigned ml = elv.m;
           const float dx = ej.x - el.x, dy = ej.y - el.y, dz = ej.z - el.z;
           const float v = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
           unsigned code = careful_code(v, c.e2lo, c.e2hi, nb, g.ka, g.kb);
@@ -639,8 +644,8 @@ __device__ __noinline__ void cold_drain(Cold& c, int lb, int k3, int qn) {
             ++c.n_exact_tri;
             exact = true;
             xe.ai = c.ai;
-            xe.pj = c.l2.p[j];
-            xe.pl = c.l3.p[l];
+            xe.pj = ejv.p;
+            xe.pl = elv.p;
             xe.meta = (mj >> 8) | ((ml >> 8) << 5) | ((mj & 0xffu) << 10) | ((ml & 0xffu) << 18);
           } else if (code < static_cast<unsigned>(nb)) {
             const float wprod = WEIGHTED ? (c.wa * c.l2.w[j]) * c.l3.w[l] * a.wscale : 0.0f;
@@ -763,17 +768,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_triangles(KArgs a) {
   {
     const size_t stride = static_cast<size_t>(a.kcap2) + a.kcap3;
     const size_t b2 = gw * stride, b3 = b2 + a.kcap2;
-    l2.e = a.slab_e + b2;
-    l2.f = a.slab_f + b2;
-    l2.m = a.slab_m + b2;
-    l2.p = a.slab_p + b2;
+    l2.v = a.slab_e + b2;
     l2.w = a.slab_w ? a.slab_w + b2 : nullptr;
     l3 = l2;
     if (!SYM) {
-      l3.e = a.slab_e + b3;
-      l3.f = a.slab_f + b3;
-      l3.m = a.slab_m + b3;
-      l3.p = a.slab_p + b3;
+      l3.v = a.slab_e + b3;
       l3.w = a.slab_w ? a.slab_w + b3 : nullptr;
     }
   }
@@ -971,30 +970,28 @@ __global__ void __launch_bounds__(kThreads, 1) k_triangles(KArgs a) {
     }
 
     // ---- Phase A: neighbour lists (in global memory, this warp's slab). A
-    // list holds at most cap - 1 entries; the entry after its last one is
-    // the padding row. The slots' points stream past in rounds of 32 (each
-    // round's cell-local FP32 points loaded two rounds ahead); a prefilter
-    // drops those certainly out of range and puts the others in the warp's
-    // ring of pending points. Whenever 32 are pending they are settled one
-    // per lane: 32 independent FP64 position loads in flight at once, then
-    // the exact offset, its classification and the append to the list.
+    // list holds at most cap - kListPad entries; the kListPad entries after
+    // its last one are padding rows. The slots' points stream past in rounds
+    // of 32 (each round's cell-local FP32 points loaded two rounds ahead); a
+    // prefilter drops those certainly out of range and puts the others in
+    // the warp's ring of pending points. Whenever 32 are pending they are
+    // settled one per lane: 32 independent FP64 position loads in flight at
+    // once, then the exact offset, its classification and the append to the
+    // list.
     auto build = [&](const Catalog& cat, const int* pre, const int* stt, ListView& lv, int cap) -> int {
       const int total = pre[27];
       const int rounded = (total + 31) & ~31;
       int cnt = 0;
-      cap -= 1;
+      cap -= kListPad;
       unsigned head = 0, pend = 0;  // ring position of the oldest pending point; pending points
       auto settle = [&](int n) {
         __syncwarp();  // the ring entries written by all lanes are visible
         bool acc = false;
-        float4 ent;
-        RowAux aux;
-        unsigned meta = 0;
+        ListEnt ent;
         float wv = 0.0f;
-        int j = 0;
         if (lane < n) {
           const unsigned slot_i = (head + static_cast<unsigned>(lane)) & (kRing - 1);
-          j = st.ring_j[slot_i];
+          const int j = st.ring_j[slot_i];
           const int s = st.ring_s[slot_i];
           // Exact anchor-relative offset of the image (FP64), rounded once.
           const double4_16a p = cat.pd[j];
@@ -1018,10 +1015,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_triangles(KArgs a) {
           if (code < static_cast<unsigned>(nb)) {
             acc = true;
             const float rho = __fsqrt_rn(v);
-            ent = make_float4(dx, dy, dz, __fmul_rn(rho, rho));
-            aux.a2r = 2.0f * rho;
-            aux.key = code * kj_mul;
-            meta = code | (static_cast<unsigned>(s) << 8);
+            ent.e = make_float4(dx, dy, dz, __fmul_rn(rho, rho));
+            ent.a2r = 2.0f * rho;
+            ent.key = code * kj_mul;
+            ent.m = code | (static_cast<unsigned>(s) << 8);
+            ent.p = j;
             wv = __double2float_rn(p.w);
           }
         }
@@ -1029,10 +1027,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_triangles(KArgs a) {
         if (acc) {
           const int e = cnt + __popc(bal & lt_mask);
           if (e < cap) {
-            lv.e[e] = ent;
-            lv.f[e] = aux;
-            lv.m[e] = meta;
-            lv.p[e] = j;
+            lv.v[e] = ent;
             if (WEIGHTED) lv.w[e] = wv;
           } else {
             atomicOr(a.flags, kFlagListOverflow);
@@ -1089,14 +1084,19 @@ __global__ void __launch_bounds__(kThreads, 1) k_triangles(KArgs a) {
     };
     const int k2 = build(it.c2, st.pre2, st.start2, l2, a.kcap2);
     const int k3 = SYM ? k2 : build(it.c3, st.pre3, st.start3, l3, a.kcap3);
-    if (lane == 0) {
-      // The padding row after the rows: rho = 1e18 gives v >= 1e36 against
+    if (lane < kListPad) {
+      // Padding rows after the rows: rho = 1e18 gives v >= 1e36 against
       // every column, rejected by the table, with a margin test that holds;
-      // so it adds into sink bins and is never flagged. Row loops that run
-      // past their last row read it instead of testing for the end.
-      l2.e[k2] = make_float4(0.0f, 0.0f, 0.0f, 1.0e36f);
-      l2.f[k2] = RowAux{2.0e18f, 0u};
-      if (WEIGHTED) l2.w[k2] = 0.0f;
+      // so they add into sink bins and are never flagged. Row loops that run
+      // past their last row read them instead of testing for the end.
+      ListEnt pad;
+      pad.e = make_float4(0.0f, 0.0f, 0.0f, 1.0e36f);
+      pad.a2r = 2.0e18f;
+      pad.key = 0u;
+      pad.m = 0u;
+      pad.p = 0;
+      l2.v[k2 + lane] = pad;
+      if (WEIGHTED) l2.w[k2 + lane] = 0.0f;
     }
     __syncwarp();  // the lists written by all lanes are visible to all lanes
     {
@@ -1143,9 +1143,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_triangles(KArgs a) {
       for (int r = 0; r < kReg; ++r) {
         const int l = lb + r * 32 + lane;
         if (l < k3) {
-          const float4 e = l3.e[l];
-          col.l[r] = make_float4(-2.0f * e.x, -2.0f * e.y, -2.0f * e.z, 0.5f * l3.f[l].a2r);
-          col.k[r] = (l3.m[l] & 0xffu) * kl_mul + col_base;
+          const ListEnt& ce = l3.v[l];
+          const float4 e = ce.e;
+          col.l[r] = make_float4(-2.0f * e.x, -2.0f * e.y, -2.0f * e.z, 0.5f * ce.a2r);
+          col.k[r] = (ce.m & 0xffu) * kl_mul + col_base;
           wl[r] = WEIGHTED ? l3.w[l] : 0.0f;
         } else {
           col.l[r] = make_float4(0.0f, 0.0f, 0.0f, 1.0e18f);
@@ -1153,26 +1154,42 @@ __global__ void __launch_bounds__(kThreads, 1) k_triangles(KArgs a) {
           wl[r] = 0.0f;
         }
       }
-      auto make_row = [&](const float4& e, const RowAux& f) {
+      // A row in registers: offset and rho^2, then 2 rho and key (one 16-
+      // and one 8-byte load), and the weight.
+      struct RowReg {
+        float4 e;
+        uint2 fk;
+        float w;
+      };
+      auto load_row = [&](const ListEnt* rp, const float* wp, RowReg& x) {
+        x.e = rp->e;
+        x.fk = *reinterpret_cast<const uint2*>(&rp->a2r);
+        x.w = WEIGHTED ? *wp : 0.0f;
+      };
+      auto make_row = [&](const RowReg& x) {
         RowV r;
-        r.x = e.x;
-        r.y = e.y;
-        r.z = e.z;
-        r.a = e.w;
-        r.a2r = f.a2r;
-        r.key = f.key;
+        r.x = x.e.x;
+        r.y = x.e.y;
+        r.z = x.e.z;
+        r.a = x.e.w;
+        r.a2r = __uint_as_float(x.fk.x);
+        r.key = x.fk.y;
         return r;
       };
       // The careful queue: entries of this tile, settled when it fills and
       // at the end of the tile (format at kKindRot).
+      // Every enqueue finds room for 32 entries: make_room settles the queue
+      // when it has less, and it is called outside the row loops (a call
+      // inside them would keep the rows in flight in local memory).
       int qn = 0;
-      auto enqueue = [&](unsigned q, unsigned tag) {
-        const unsigned bal = __ballot_sync(FULL, q != 0u);
-        if (bal == 0u) return;
+      auto make_room = [&]() {
         if (qn + 32 > kQueueCap) {
           cold_drain<SURVEY, WEIGHTED, HG>(c, lb, k3, qn);
           qn = 0;
         }
+      };
+      auto enqueue = [&](unsigned q, unsigned tag) {
+        const unsigned bal = __ballot_sync(FULL, q != 0u);
         if (q) c.queue[qn + __popc(bal & lt_mask)] = (static_cast<unsigned long long>(q) << 32) | tag;
         qn += __popc(bal);
       };
@@ -1192,60 +1209,61 @@ __global__ void __launch_bounds__(kThreads, 1) k_triangles(KArgs a) {
         }
       };
       // One row against column slots 0..N-1.
-      auto row_at = [&](const float4& e, const RowAux& f, float wj, unsigned rbit, auto n_tag, unsigned& q) {
+      auto row_at = [&](const RowReg& x, unsigned rbit, auto n_tag, unsigned& q) {
         constexpr int N = decltype(n_tag)::value;
-        const RowV r = make_row(e, f);
+        const RowV r = make_row(x);
         if (WEIGHTED || HG) {
 #pragma unroll
-          for (int s = 0; s < N; ++s) cand_slow(r, col.l[s], col.k[s], wl[s], 1u, wj, rbit, q);
+          for (int s = 0; s < N; ++s) cand_slow(r, col.l[s], col.k[s], wl[s], 1u, x.w, rbit, q);
         } else {
           row_full<N>(r, col, bk, rbit, q);
         }
       };
-      // Rows [jb, je) of one flag group against column slots 0..N-1, R rows
-      // per iteration; a row position at or past je reads the padding row
-      // (index k2), which only adds into sinks, so the loop has no remainder
-      // test. The bodies' "memory" clobber keeps the compiler from hoisting
-      // loads above a body, so each row's registers are reloaded with the row
-      // R positions ahead right after its body: the load has the next R - 1
-      // bodies' time to land, and no register is copied.
-      auto rows = [&](int jb, int je, auto n_tag, unsigned& q) {
+      // Rows j0 .. j1 - 1 against column slots 0..N-1, R rows per iteration.
+      // A range ends at k2 or holds a multiple of R rows, so the rows an
+      // iteration takes past j1 are padding rows, which only add into sinks:
+      // the loop has no remainder test. The bodies' "memory" clobber keeps
+      // the compiler from hoisting loads above a body, so each row's
+      // registers are reloaded with the row R positions ahead right after its
+      // body (immediate offsets from one row pointer): the load has the next
+      // R - 1 bodies' time to land, and no register is copied. The flag word
+      // covers groups of `group` rows (8, 16 or 32, a multiple of R); after
+      // each group it is queued, and when the queue is nearly full the loop
+      // stops at that group boundary, the queue is settled and the loop
+      // resumes there.
+      auto run_rows = [&](int j0, int j1, auto n_tag) {
         constexpr int N = decltype(n_tag)::value;
         constexpr int R = N == kReg ? 4 : 2;
-        float4 e[R];
-        RowAux f[R];
-        float w[R];
+        int j = j0;
+        while (j < j1) {
+          make_room();
+          const ListEnt* rp = l2.v + j;
+          const float* wp = WEIGHTED ? l2.w + j : nullptr;
+          RowReg x[R];
 #pragma unroll
-        for (int p = 0; p < R; ++p) {
-          const int jj = jb + p < je ? jb + p : k2;
-          e[p] = l2.e[jj];
-          f[p] = l2.f[jj];
-          w[p] = WEIGHTED ? l2.w[jj] : 0.0f;
-        }
+          for (int p = 0; p < R; ++p) load_row(rp + p, wp + p, x[p]);
+          unsigned q = 0, rb = 1u;
+          int jg = j;
 #pragma unroll 1
-        for (int j = jb; j < je; j += R) {
+          while (j < j1) {
 #pragma unroll
-          for (int p = 0; p < R; ++p) {
-            row_at(e[p], f[p], w[p], 1u << ((j + p - jb) & 31), n_tag, q);
-            const int jj = j + R + p < je ? j + R + p : k2;
-            e[p] = l2.e[jj];
-            f[p] = l2.f[jj];
-            w[p] = WEIGHTED ? l2.w[jj] : 0.0f;
+            for (int p = 0; p < R; ++p) {
+              row_at(x[p], rb << p, n_tag, q);
+              load_row(rp + R + p, wp + R + p, x[p]);
+            }
+            rp += R;
+            if (WEIGHTED) wp += R;
+            j += R;
+            rb <<= R;
+            if (j - jg >= group || j >= j1) {
+              enqueue(q, (static_cast<unsigned>(jg) << 8) | (static_cast<unsigned>(N - 1) << 5) |
+                             static_cast<unsigned>(lane));
+              q = 0;
+              rb = 1u;
+              jg = j;
+              if (qn + 32 > kQueueCap) break;
+            }
           }
-        }
-      };
-      // Rows [j0, j1) against column slots 0..N-1, in groups of `group` rows
-      // (8, 16 or 32: a group never straddles a 32-row block), each group's
-      // flag words queued after it.
-      auto groups = [&](int j0, int j1, auto n_tag) {
-        constexpr int N = decltype(n_tag)::value;
-#pragma unroll 1
-        for (int jb = j0; jb < j1; jb += group) {
-          const int je = min(jb + group, j1);
-          unsigned q = 0;
-          rows(jb, je, n_tag, q);
-          enqueue(q, (static_cast<unsigned>(jb) << 8) | (static_cast<unsigned>(N - 1) << 5) |
-                         static_cast<unsigned>(lane));
         }
       };
       if (SYM) {
@@ -1258,9 +1276,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_triangles(KArgs a) {
 #pragma unroll 1
         for (int S = 0; S * 32 < m; ++S) {
           const int bb = lb + 32 * S, be = min(bb + 32, k2);
-          if (S == 1) groups(bb, be, std::integral_constant<int, 1>());
-          if (S == 2) groups(bb, be, std::integral_constant<int, 2>());
-          if (S == 3) groups(bb, be, std::integral_constant<int, 3>());
+          if (S == 1) run_rows(bb, be, std::integral_constant<int, 1>());
+          if (S == 2) run_rows(bb, be, std::integral_constant<int, 2>());
+          if (S == 3) run_rows(bb, be, std::integral_constant<int, 3>());
           float4 cl = col.l[0];
           unsigned ck = col.k[0];
           float cw = wl[0];
@@ -1272,48 +1290,60 @@ __global__ void __launch_bounds__(kThreads, 1) k_triangles(KArgs a) {
               cw = wl[s];
             }
           }
-          const bool cval = bb + lane < k2;
-          unsigned qd = 0;
-          // Each lane's rows of steps d and d + 1 are in flight; a row
-          // position past the list reads the padding row (masked anyway).
-          auto rot_row = [&](int d) {
-            const int rr = bb + ((lane + d) & 31);
-            return rr < k2 ? rr : k2;
+          // Each lane's rows of steps d and d + 1 are in flight (block
+          // positions past the list read stale entries of the slab, masked).
+          const ListEnt* bp = l2.v + bb;
+          const float* bw = WEIGHTED ? l2.w + bb : nullptr;
+          auto rot_load = [&](int d, RowReg& x) {
+            const int o = (lane + d) & 31;
+            load_row(bp + o, bw + o, x);
           };
-          float4 re[2];
-          RowAux rf[2];
-          float rw[2];
-#pragma unroll
-          for (int p = 0; p < 2; ++p) {
-            const int jj = rot_row(1 + p);
-            re[p] = l2.e[jj];
-            rf[p] = l2.f[jj];
-            rw[p] = WEIGHTED ? l2.w[jj] : 0.0f;
-          }
+          auto rot_cand = [&](const RowReg& x, int d, unsigned in, bool masked, unsigned& q) {
+            const RowV r = make_row(x);
+            const unsigned rbit = 1u << (d - 1);
+            if (WEIGHTED || HG)
+              cand_slow(r, cl, ck, cw, in, x.w, rbit, q);
+            else if (masked)
+              row_rot1(r, cl, ck, bk, rbit, in, q);
+            else
+              row_rot1_full(r, cl, ck, bk, rbit, q);
+          };
+          unsigned qd = 0;
+          RowReg x[2];
+          rot_load(1, x[0]);
+          rot_load(2, x[1]);
+          if (be - bb == 32) {
+            // A full block: every lane's pair is one to count, except that
+            // d = 16 pairs lanes L and L + 16 twice.
 #pragma unroll 1
-          for (int d0 = 1; d0 <= 16; d0 += 2) {
+            for (int d0 = 1; d0 < 15; d0 += 2) {
 #pragma unroll
-            for (int p = 0; p < 2; ++p) {
-              const int d = d0 + p;
-              const int rr = bb + ((lane + d) & 31);
-              const unsigned in = (cval && rr < k2 && (d < 16 || lane < 16)) ? 1u : 0u;
-              const RowV r = make_row(re[p], rf[p]);
-              const unsigned rbit = 1u << (d - 1);
-              if (WEIGHTED || HG)
-                cand_slow(r, cl, ck, cw, in, rw[p], rbit, qd);
-              else
-                row_rot1(r, cl, ck, bk, rbit, in, qd);
-              const int jj = rot_row(d + 2);
-              re[p] = l2.e[jj];
-              rf[p] = l2.f[jj];
-              rw[p] = WEIGHTED ? l2.w[jj] : 0.0f;
+              for (int p = 0; p < 2; ++p) {
+                rot_cand(x[p], d0 + p, 1u, false, qd);
+                rot_load(d0 + p + 2, x[p]);
+              }
+            }
+            rot_cand(x[0], 15, 1u, false, qd);
+            rot_cand(x[1], 16, lane < 16 ? 1u : 0u, true, qd);
+          } else {
+            const bool cval = bb + lane < k2;
+#pragma unroll 1
+            for (int d0 = 1; d0 <= 16; d0 += 2) {
+#pragma unroll
+              for (int p = 0; p < 2; ++p) {
+                const int d = d0 + p;
+                const int rr = bb + ((lane + d) & 31);
+                rot_cand(x[p], d, (cval && rr < k2 && (d < 16 || lane < 16)) ? 1u : 0u, true, qd);
+                rot_load(d + 2, x[p]);
+              }
             }
           }
+          make_room();
           enqueue(qd, (static_cast<unsigned>(bb) << 8) | (kKindRot << 5) | static_cast<unsigned>(lane));
         }
-        groups(lb + kTile, k2, std::integral_constant<int, kReg>());
+        run_rows(lb + kTile, k2, std::integral_constant<int, kReg>());
       } else {
-        groups(0, k2, std::integral_constant<int, kReg>());
+        run_rows(0, k2, std::integral_constant<int, kReg>());
       }
       if (qn > 0) cold_drain<SURVEY, WEIGHTED, HG>(c, lb, k3, qn);
     }
