@@ -287,7 +287,7 @@ __device__ __forceinline__ void add128(unsigned long long* w, long long v) {
 // Constants of the candidate bodies, fixed per launch.
 struct BodyK {
   float tscale, hm;
-  unsigned tab_adj, tab_last, car, dummy;
+  unsigned tab_adj, tab_last, car, dummy, nb_cs;
 };
 // One row: offset, rho^2, 2 rho, key.
 struct RowV {
@@ -366,11 +366,13 @@ __device__ __forceinline__ void row_rot1_full(const RowV& r, const float4& l, un
 // %1-%3 d_j, %4 rho_j^2, %5 2 rho_j, %6-%8 -2 d_l, %9 rho_l, %10 row key,
 // %11 column key, %12 mask, %13 table scale, %14/%15 table bias and last
 // entry, %16 the careful code, %17 -M, %18 dummy, %19 row weight, %20 column
-// weight, %21 rbit. Rejected and careful codes address sink bins, as in the
-// count bodies.
+// weight, %21 rbit, %22 nb * code scale. Unlike the count bodies, only a
+// candidate with a bin code adds into the histogram; the others add to the
+// lane's scratch word. Rejected candidates are common, and their returning,
+// per-lane-valued atomics on the few reject-sink words would serialize.
 __device__ __forceinline__ void cand_wsum(const RowV& r, const float4& l, unsigned kl, unsigned in, const BodyK& k,
                                           float wrow, float wl, unsigned rbit, unsigned& q) {
-  asm volatile("{\n\t.reg .pred inp;\n\t" NCORR_DECL(0)
+  asm volatile("{\n\t.reg .pred inp, ok, nmg;\n\t" NCORR_DECL(0)
                ".reg .f32 wp;\n\t.reg .b32 wi, whi, wold, wnew, wcy, adrh;\n\t"
                "mul.rn.f32 pp0, %1, %6;\n\t"
                "fma.rn.f32 pp0, %2, %7, pp0;\n\t"
@@ -384,8 +386,11 @@ __device__ __forceinline__ void cand_wsum(const RowV& r, const float4& l, unsign
                "abs.f32 t0, pp0;\n\t"
                "fma.rn.f32 H0, %5, %9, %17;\n\t"
                "setp.ne.u32 inp, %12, 0;\n\t"
-               "setp.lt.and.f32 upd0, t0, H0, inp;\n\t"
-               "setp.eq.or.u32 w0, code0, %16, !upd0;\n\t"
+               "setp.lt.u32 ok, code0, %22;\n\t"
+               "and.pred ok, ok, inp;\n\t"
+               "setp.lt.and.f32 upd0, t0, H0, ok;\n\t"
+               "setp.ge.and.f32 nmg, t0, H0, ok;\n\t"
+               "setp.eq.or.u32 w0, code0, %16, nmg;\n\t"
                "and.pred w0, w0, inp;\n\t"
                "@w0 or.b32 %0, %0, %21;\n\t"
                "add.u32 key0, %10, %11;\n\t"
@@ -404,7 +409,7 @@ __device__ __forceinline__ void cand_wsum(const RowV& r, const float4& l, unsign
                : "+r"(q)
                : "f"(r.x), "f"(r.y), "f"(r.z), "f"(r.a), "f"(r.a2r), "f"(l.x), "f"(l.y), "f"(l.z), "f"(l.w),
                  "r"(r.key), "r"(kl), "r"(in), "f"(k.tscale), "r"(k.tab_adj), "r"(k.tab_last), "r"(k.car),
-                 "f"(k.hm), "r"(k.dummy), "f"(wrow), "f"(wl), "r"(rbit)
+                 "f"(k.hm), "r"(k.dummy), "f"(wrow), "f"(wl), "r"(rbit), "r"(k.nb_cs)
                : "memory");
 }
 
@@ -811,6 +816,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_triangles(KArgs a) {
     bk.tab_adj = tab_sh - 0x4B000000u;
     bk.tab_last = tab_sh + static_cast<unsigned>(g.tab_n - 1);
     bk.car = car;
+    bk.nb_cs = nb_cs;
     bk.dummy = static_cast<unsigned>(__cvta_generic_to_shared(smem + L.scratch)) + 8u * lane;
     bk.tscale = g.tab_scale;
     bk.hm = g.hm;
