@@ -22,7 +22,7 @@ constexpr int kReg = 4;          // list entries per lane held in registers
 constexpr int kTile = 32 * kReg; // column tile of the pair loop
 constexpr int kQueueCap = 256;   // per-warp queue of careful/exact-path candidates
 #ifndef NCORR_TABLE_SIZE
-#define NCORR_TABLE_SIZE 32768
+#define NCORR_TABLE_SIZE 65536
 #endif
 constexpr int kTableSize = NCORR_TABLE_SIZE;  // bin table entries (u8)
 
@@ -35,6 +35,16 @@ constexpr unsigned kCodeCareful = 0xFFu;
 // careful candidates add into (the bin table's codes for them), so the
 // candidate bodies need not test the code. Nothing reads the sinks.
 __host__ __device__ inline int hist_row(int nb) { return nb + 2; }
+__host__ __device__ inline int hist_words(int nb) { return nb * nb * hist_row(nb); }
+// Bin-table codes of "reject" and "careful": with a CTA histogram (code
+// scale = the byte stride of a bin, > 1) the two sink bins of the row; with
+// the global histogram (code scale 1) the plain markers above.
+__host__ __device__ inline unsigned table_code_reject(int nb, int cs) {
+  return cs > 1 ? static_cast<unsigned>(nb * cs) : kCodeReject;
+}
+__host__ __device__ inline unsigned table_code_careful(int nb, int cs) {
+  return cs > 1 ? static_cast<unsigned>((nb + 1) * cs) : kCodeCareful;
+}
 
 // One neighbour-list entry of the triangle kernel (32 bytes): the offset d
 // from the anchor and rho^2 (rho = sqrt_rn of the r1^2 estimate), then what
@@ -51,16 +61,6 @@ struct __align__(16) ListEnt {
 // Padding records after each list: a row loop that runs up to this many rows
 // past the list's end reads padding rows, which add into sink bins only.
 constexpr int kListPad = 8;
-__host__ __device__ inline int hist_words(int nb) { return nb * nb * hist_row(nb); }
-// Bin-table codes of "reject" and "careful": with a CTA histogram (code
-// scale = the byte stride of a bin, > 1) the two sink bins of the row; with
-// the global histogram (code scale 1) the plain markers above.
-__host__ __device__ inline unsigned table_code_reject(int nb, int cs) {
-  return cs > 1 ? static_cast<unsigned>(nb * cs) : kCodeReject;
-}
-__host__ __device__ inline unsigned table_code_careful(int nb, int cs) {
-  return cs > 1 ? static_cast<unsigned>((nb + 1) * cs) : kCodeCareful;
-}
 
 // Error flags written by kernels.
 constexpr int kFlagOutOfGrid = 1;     // a point the reference would index out of bounds
