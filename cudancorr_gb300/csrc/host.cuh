@@ -171,7 +171,7 @@ struct ncorr_handle {
   // weight of the last call's triangles indexed past triCountsAll_.
   ncorr_gb300::RppiGeom rg;
   std::vector<double> pi_bins_out;
-  ncorr_host::DevBuf rp_pos, rp_ab, rp_rel, rp_meta;
+  ncorr_host::DevBuf rp_pos, rp_ab, rp_rel, rp_meta, rp_pw;
   double rppi_overflow = 0.0;
 };
 

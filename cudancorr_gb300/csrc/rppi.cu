@@ -3,23 +3,28 @@
 // restates countTrianglesRppiBox / countTrianglesRppiSurvey
 // (source/device.cu:317-379, :434-505 of cudaNcorr) operation for operation.
 //
-// One CTA of 256 threads owns one anchor at a time (taken from a global
-// counter). Phase A walks the 27 (cell, image) slots of the anchor's home
-// cell, flattened over the CTA's threads, and keeps the points that pass the
-// reference's cut against the anchor: box pi^2 < piMax^2 and rpMin^2 < rp^2 <
-// rpMax^2, survey 0 < s^2 < rpMax^2 + piMax^2. That cut is the same test for
-// the kernel's p2 and p3 roles, so a list per distinct catalogue serves both.
-// Phase B takes the list pairs (one row per warp, lanes over the row). An
-// FP32 estimate from anchor-relative offsets drops pairs that are certainly
-// cut. In a box, the FP32 classifier of rppi_fast.cuh then settles almost
-// every pair with rigorous error bands; the pairs it leaves uncertain, and
-// every survey pair, are evaluated in FP64 with the reference's operations
-// and contractions, sorted and binned as getTriangleIndexRppi does
-// (source/device.cu:203-255). Each counted triangle is added to the global
-// histogram with one atomic. With p2 == p3 in a box, each unordered pair is visited once: its
-// two orderings give the same index unless two sides tie in rp^2 (the
-// reference's swap order then decides which pi goes with which side), and
-// the tie case computes both.
+// One warp owns one anchor at a time; warps take anchors four at a time, in
+// cell order, from a global counter, so consecutive anchors of a warp share
+// their 27 (cell, image) slots. The GPU's FP64 pipe is a small fraction of
+// its FP32 rate, so FP64 work only ever runs 32 lanes wide: FP32 estimates
+// with rigorous bounds decide what they can, and what they leave waits in a
+// per-warp ring in shared memory until 32 items are ready.
+// Phase A walks the slots' points (FP32 copies, 32 per round); points that
+// the FP32 estimate does not certainly cut are settled in FP64 against the
+// reference's cut: box pi^2 < piMax^2 and rpMin^2 < rp^2 < rpMax^2, survey
+// 0 < s^2 < rpMax^2 + piMax^2. That cut is the same test for the kernel's p2
+// and p3 roles, so a list per distinct catalogue serves both.
+// Phase B enumerates the list pairs flattened over the lanes (pairs j < l
+// when p2 == p3 in a box, all ordered pairs otherwise). In a box, the FP32
+// classifier of rppi_fast.cuh settles almost every pair with rigorous error
+// bands; the pairs it leaves uncertain, and every survey pair that an FP32
+// estimate does not certainly cut, are evaluated in FP64 with the
+// reference's operations and contractions, sorted and binned as
+// getTriangleIndexRppi does (source/device.cu:203-255). Each counted
+// triangle is added to the global histogram with one atomic. With p2 == p3
+// in a box, each unordered pair is visited once: its two orderings give the
+// same index unless two sides tie in rp^2 (the reference's swap order then
+// decides which pi goes with which side), and the tie case computes both.
 #include "host.cuh"
 
 namespace ncorr_gb300 {
@@ -126,61 +131,305 @@ __global__ void k_rp_assign(const double4_16a* __restrict__ in, int n, RppiGeom 
   if ((threadIdx.x & 31) == 0 && f) atomicOr(flags, f);
 }
 
+// Cell-ordered copy of the points, and an FP32 copy (each coordinate rounded
+// once) carrying the point's cell id.
 __global__ void k_rp_scatter(const double4_16a* __restrict__ in, int n, const int* __restrict__ cid,
-                             int* __restrict__ cursor, double4_16a* __restrict__ pd) {
+                             int* __restrict__ cursor, double4_16a* __restrict__ pd, float4* __restrict__ pq) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int c = cid[i];
   if (c < 0) return;
-  pd[atomicAdd(&cursor[c], 1)] = in[i];
+  const double4_16a p = in[i];
+  const int k = atomicAdd(&cursor[c], 1);
+  pd[k] = p;
+  pq[k] = make_float4(__double2float_rn(p.x), __double2float_rn(p.y), __double2float_rn(p.z), __int_as_float(c));
 }
 
 constexpr int kRppiThreads = 256;
+constexpr int kRppiWarps = kRppiThreads / 32;
+constexpr int kRppiChunk = 4;  // consecutive anchors a warp takes per counter increment
+constexpr int kRppiRing = 64;  // per-warp ring of points or pairs awaiting FP64
+constexpr unsigned kRppiFull = 0xffffffffu;
 
-// Phase A for one catalogue: the 27 slots flattened over the CTA's threads.
-// s_off[27] holds the slots' prefix sums, s_cell/s_sh their cell ids and
-// image shifts (box).
-__device__ __forceinline__ void rppi_gather(const RppiArgs& a, const double4_16a& p1, const double4_16a* pd,
-                                            const int* start, const int* s_off, const int* s_cell,
-                                            const double (*s_sh)[3], int total, int* s_n, double4_16a* pos,
-                                            double2* ab, float4* rel, unsigned* meta, const double* sb, int cap) {
+// One catalogue's 27 (cell, image) slots around a home cell, slot s in lane
+// s: the FP32 image shift (x, y, z) and, in .w (int bits), the slot's first
+// point less its offset in the flattened walk; `code` the shift's signs
+// (two bits per axis, sign + 1).
+struct RppiSlots {
+  float4 f[32];
+  int code[32];
+};
+
+struct RppiWarpSm {
+  RppiSlots s2, s3;
+  int2 ring[kRppiRing];
+};
+
+// One per-warp list (per-catalogue neighbours of the current anchor).
+struct RppiList {
+  double4_16a* pos;
+  double2* ab;
+  float4* rel;
+  unsigned* meta;
+  double* pw;
+};
+
+__device__ __forceinline__ double rppi_shift(int code, int d, double box) {
+  const int s = ((code >> (2 * d)) & 3) - 1;
+  return s == 0 ? 0.0 : (s > 0 ? box : -box);
+}
+
+// Anchor cell (initCellIndexBox / initCellIndexSurvey, source/device.cu:75-87:
+// the cell id k_rp_assign gave the anchor, which is clamped in a box and
+// never on the upper face in a survey) and its 27 slots (shiftCellIndexBox /
+// Survey, :89-153) in the reference's i, j, k order. Returns the slots'
+// total point count; `excl` gets the lane's exclusive offset (0x7fffffff
+// past slot 26, so that rppi_slot_of never picks those lanes).
+template <bool SURVEY>
+__device__ __forceinline__ int rppi_slots(const RppiGeom& g, int hc, const int* count, const int* start,
+                                          RppiSlots& sl, int lane, int& excl) {
+  const int h[3] = {hc / (g.nc[1] * g.nc[2]), (hc / g.nc[2]) % g.nc[1], hc % g.nc[2]};
+  int cnt = 0, first = 0, code = 0;
+  float sh[3] = {0.0f, 0.0f, 0.0f};
+  if (lane < 27) {
+    const int sd[3] = {lane / 9 - 1, (lane / 3) % 3 - 1, lane % 3 - 1};
+    int c[3];
+    bool ok = true;
+    for (int d = 0; d < 3; ++d) {
+      c[d] = h[d] + sd[d];
+      int s = 0;
+      if (SURVEY) {
+        if (c[d] == g.nc[d] || c[d] == -1) ok = false;
+      } else if (c[d] == g.nc[d]) {
+        c[d] = 0;
+        s = 1;
+      } else if (c[d] == -1) {
+        c[d] = g.nc[d] - 1;
+        s = -1;
+      }
+      code |= (s + 1) << (2 * d);
+      sh[d] = s == 0 ? 0.0f : (s > 0 ? g.fbox[d] : -g.fbox[d]);
+    }
+    if (ok) {
+      const int cell = c[2] + g.nc[2] * (c[1] + g.nc[1] * c[0]);
+      cnt = count[cell];
+      first = start[cell];
+    }
+  }
+  int incl = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(kRppiFull, incl, o);
+    if (lane >= o) incl += v;
+  }
+  excl = lane < 27 ? incl - cnt : 0x7fffffff;
+  __syncwarp();  // the previous table is no longer read
+  sl.f[lane] = make_float4(sh[0], sh[1], sh[2], __int_as_float(first - (incl - cnt)));
+  sl.code[lane] = code;
+  __syncwarp();
+  return __shfl_sync(kRppiFull, incl, 26);
+}
+
+// The slot of flattened position t: the largest s with excl[s] <= t.
+__device__ __forceinline__ int rppi_slot_of(int excl, int t) {
+  int s = 0;
+#pragma unroll
+  for (int step = 16; step; step >>= 1)
+    if (__shfl_sync(kRppiFull, excl, s + step) <= t) s += step;
+  return s;
+}
+
+// FP64 settling of up to 32 ring entries (point index, shift code), one per
+// lane, against the reference's cut. Kept points are appended to the list
+// from position n on; returns the new count (entries past `cap` are not
+// written and raise `overflow`).
+template <bool SURVEY, bool WEIGHTED>
+__device__ __forceinline__ int rppi_settle(const RppiArgs& a, const double4_16a& p1, const double4_16a* pd,
+                                           int2 e, bool act, const RppiList& L, int n, const double* sb, int lane,
+                                           bool& overflow) {
   const RppiGeom& g = a.g;
-  for (int t = threadIdx.x; t < total; t += blockDim.x) {
-    int s = 0;
-    while (s < 26 && t >= s_off[s + 1]) ++s;
-    double4_16a q = pd[start[s_cell[s]] + (t - s_off[s])];
-    double x, y;
-    bool keep;
-    if (g.survey) {
-      x = sqr_sep_exact(p1.x, p1.y, p1.z, q.x, q.y, q.z, g.fma_pattern);
-      y = 0.0;
+  bool keep = false;
+  double4_16a q = {0.0, 0.0, 0.0, 0.0};
+  double x = 0.0, y = 0.0, dx = 0.0, dy = 0.0, dz = 0.0;
+  if (act) {
+    q = pd[e.x];
+    if (!SURVEY) {
+      // particle2.x += rShift2.x (source/device.cu:334-336)
+      q.x = __dadd_rn(q.x, rppi_shift(e.y, 0, g.box[0]));
+      q.y = __dadd_rn(q.y, rppi_shift(e.y, 1, g.box[1]));
+      q.z = __dadd_rn(q.z, rppi_shift(e.y, 2, g.box[2]));
+    }
+    dx = __dsub_rn(p1.x, q.x);
+    dy = __dsub_rn(p1.y, q.y);
+    dz = __dsub_rn(p1.z, q.z);
+    if (SURVEY) {
+      x = sqr_sum_exact(dx, dy, dz, g.fma_pattern);  // sqrSep(p1, q)
       keep = x < g.sqr_rmax && x > g.sqr_rmin;
     } else {
-      // particle2.x += rShift2.x (source/device.cu:334-336)
-      q.x = __dadd_rn(q.x, s_sh[s][0]);
-      q.y = __dadd_rn(q.y, s_sh[s][1]);
-      q.z = __dadd_rn(q.z, s_sh[s][2]);
-      const double dz = __dsub_rn(p1.z, q.z);
       y = __dmul_rn(dz, dz);
-      x = rp_exact(__dsub_rn(p1.x, q.x), __dsub_rn(p1.y, q.y), g.rp_pattern);
+      x = rp_exact(dx, dy, g.rp_pattern);
       keep = y < g.sqr_pimax && x < g.sqr_rpmax && x > g.sqr_rpmin;
     }
-    if (keep) {
-      const int k = atomicAdd(s_n, 1);
-      if (k < cap) {
-        pos[k] = q;
-        ab[k] = make_double2(x, y);
-        // Box: the classifier's per-side inputs, sqrt_rn(fl32(rp^2)) and the
-        // exact rp and pi bins (floor(sqrtf(pi^2)) as the reference forms it).
-        const float rho = g.survey ? 0.0f : __fsqrt_rn(__double2float_rn(x));
-        rel[k] = make_float4(__double2float_rn(__dsub_rn(q.x, p1.x)), __double2float_rn(__dsub_rn(q.y, p1.y)),
-                             __double2float_rn(__dsub_rn(q.z, p1.z)), rho);
-        if (!g.survey)
-          meta[k] = static_cast<unsigned>(exact_bin(x, sb, g.nb)) |
+  }
+  const unsigned km = __ballot_sync(kRppiFull, keep);
+  if (keep) {
+    const int k = n + __popc(km & ((1u << lane) - 1u));
+    if (k < a.cap) {
+      L.pos[k] = q;
+      L.ab[k] = make_double2(x, y);
+      // The anchor-relative offset fl32(q - p1) = -fl32(p1 - q) and, in a
+      // box, the classifier's per-side inputs: sqrt_rn(fl32(rp^2)) and the
+      // exact rp and pi bins (floor(sqrtf(pi^2)) as the reference forms it).
+      const float rho = SURVEY ? 0.0f : __fsqrt_rn(__double2float_rn(x));
+      L.rel[k] = make_float4(-__double2float_rn(dx), -__double2float_rn(dy), -__double2float_rn(dz), rho);
+      if (!SURVEY)
+        L.meta[k] = static_cast<unsigned>(exact_bin(x, sb, g.nb)) |
                     (static_cast<unsigned>(floorf(__fsqrt_rn(__double2float_rn(y)))) << 16);
+      if (WEIGHTED) L.pw[k] = __dmul_rn(p1.w, q.w);
+    } else {
+      overflow = true;
+    }
+  }
+  return n + __popc(km);
+}
+
+// Phase A for one catalogue: the warp walks the slots' points 32 at a time.
+// The FP32 estimate drops the points the reference certainly cuts (the a_*
+// thresholds); the rest wait in the ring and are settled 32 at a time.
+// Returns the number of points kept.
+template <bool SURVEY, bool WEIGHTED>
+__device__ __forceinline__ int rppi_gather(const RppiArgs& a, const double4_16a& p1, const float4& p1f,
+                                           const double4_16a* pd, const float4* pq, const RppiSlots& sl, int excl,
+                                           int total, int2* ring, const RppiList& L, const double* sb, int lane,
+                                           bool& overflow) {
+  const RppiGeom& g = a.g;
+  const unsigned lt = (1u << lane) - 1u;
+  int n = 0, head = 0, tail = 0;
+  for (int t0 = 0; t0 < total; t0 += 32) {
+    const int t = t0 + lane;
+    const int s = rppi_slot_of(excl, t);
+    bool cand = false;
+    int idx = 0;
+    if (t < total) {
+      const float4 f = sl.f[s];
+      idx = __float_as_int(f.w) + t;
+      const float4 q = pq[idx];
+      if (SURVEY) {
+        const float dx = q.x - p1f.x, dy = q.y - p1f.y, dz = q.z - p1f.z;
+        cand = fmaf(dz, dz, fmaf(dx, dx, dy * dy)) <= g.a_s_hi;
       } else {
-        atomicOr(a.flags, kFlagListOverflow);
+        const float dx = (q.x + f.x) - p1f.x, dy = (q.y + f.y) - p1f.y, dz = (q.z + f.z) - p1f.z;
+        const float rp = fmaf(dx, dx, dy * dy);
+        cand = dz * dz <= g.a_pi_hi && rp <= g.a_rp_hi && rp >= g.a_rp_lo;
       }
+    }
+    const unsigned m = __ballot_sync(kRppiFull, cand);
+    if (cand) ring[(tail + __popc(m & lt)) & (kRppiRing - 1)] = make_int2(idx, sl.code[s]);
+    tail += __popc(m);
+    if (tail - head >= 32) {
+      __syncwarp();
+      n = rppi_settle<SURVEY, WEIGHTED>(a, p1, pd, ring[(head + lane) & (kRppiRing - 1)], true, L, n, sb, lane,
+                                        overflow);
+      head += 32;
+      __syncwarp();  // these entries may be overwritten
+    }
+  }
+  if (tail > head) {
+    __syncwarp();
+    n = rppi_settle<SURVEY, WEIGHTED>(a, p1, pd, ring[(head + lane) & (kRppiRing - 1)], lane < tail - head, L, n,
+                                      sb, lane, overflow);
+    __syncwarp();
+  }
+  return n;
+}
+
+template <bool SURVEY, bool SYM, bool WEIGHTED>
+__device__ __forceinline__ void rppi_count(const RppiArgs& a, long long idx, long long idx2, double w, double w2) {
+  if (SYM && !SURVEY) {
+    if (idx2 == idx && !WEIGHTED) {
+      rppi_add<false>(a, idx, 0.0, 2ull);
+    } else {
+      rppi_add<WEIGHTED>(a, idx, w, 1ull);
+      rppi_add<WEIGHTED>(a, idx2, w2, 1ull);
+    }
+  } else {
+    rppi_add<WEIGHTED>(a, idx, w, 1ull);
+  }
+}
+
+// FP64 evaluation of one list pair (j of list 2, l of list 3) with the
+// reference's operations, and its histogram update.
+template <bool SURVEY, bool SYM, bool WEIGHTED>
+__device__ __forceinline__ void rppi_exact_pair(const RppiArgs& a, const double4_16a& p1, double o1x, int2 e,
+                                                const RppiList& L2, const RppiList& L3, const double* sb) {
+  const RppiGeom& g = a.g;
+  const double4_16a pj = L2.pos[e.x], pl = L3.pos[e.y];
+  const double2 abj = L2.ab[e.x], abl = L3.ab[e.y];
+  long long idx = -1, idx2 = -1;
+  double w = 1.0, w2 = 1.0;
+  if (!SURVEY) {
+    const double dz = __dsub_rn(pj.z, pl.z);
+    const double pi3 = __dmul_rn(dz, dz);
+    if (!(pi3 < g.sqr_pimax)) return;
+    const double rp3 = rp_exact(__dsub_rn(pj.x, pl.x), __dsub_rn(pj.y, pl.y), g.rp_pattern);
+    if (!(rp3 < g.sqr_rpmax && rp3 > g.sqr_rpmin)) return;
+    idx = rppi_index(abj.x, abl.x, rp3, abj.y, abl.y, pi3, sb, g.nb, g.npi);
+    if (idx < 0) return;
+    if (WEIGHTED) w = __dmul_rn(__dmul_rn(p1.w, pj.w), pl.w);
+    if (SYM) {
+      // The (l, j) ordering: same sides, anchor sides swapped.
+      if (abj.x == abl.x || abj.x == rp3 || abl.x == rp3)
+        idx2 = rppi_index(abl.x, abj.x, rp3, abl.y, abj.y, pi3, sb, g.nb, g.npi);
+      else
+        idx2 = idx;
+      if (WEIGHTED) w2 = __dmul_rn(__dmul_rn(p1.w, pl.w), pj.w);
+    }
+  } else {
+    const double s3 = sqr_sep_exact(pj.x, pj.y, pj.z, pl.x, pl.y, pl.z, g.fma_pattern);
+    if (!(s3 < g.sqr_rmax && s3 > g.sqr_rmin)) return;
+    // getLOS (source/device.cu:45-56): positions relative to d_ori, summed
+    // left to right.
+    const double lx = __dadd_rn(__dadd_rn(o1x, __dsub_rn(pj.x, g.ori_x)), __dsub_rn(pl.x, g.ori_x));
+    const double ly = __dadd_rn(__dadd_rn(p1.y, pj.y), pl.y);
+    const double lz = __dadd_rn(__dadd_rn(p1.z, pj.z), pl.z);
+    const double sqrL = dot3_exact(lx, ly, lz, lx, ly, lz, g.dot_pattern);
+    const double pm = __dmul_rn(g.sqr_pimax, sqrL);
+    // getSqrSdotL (source/device.cu:58-63) for (p1,p2), (p1,p3), (p2,p3).
+    double t = dot3_exact(lx, ly, lz, __dsub_rn(p1.x, pj.x), __dsub_rn(p1.y, pj.y), __dsub_rn(p1.z, pj.z),
+                          g.dot_pattern);
+    const double q1 = __dmul_rn(t, t);
+    if (pm < q1) return;
+    t = dot3_exact(lx, ly, lz, __dsub_rn(p1.x, pl.x), __dsub_rn(p1.y, pl.y), __dsub_rn(p1.z, pl.z), g.dot_pattern);
+    const double q2 = __dmul_rn(t, t);
+    if (pm < q2) return;
+    t = dot3_exact(lx, ly, lz, __dsub_rn(pj.x, pl.x), __dsub_rn(pj.y, pl.y), __dsub_rn(pj.z, pl.z), g.dot_pattern);
+    const double q3 = __dmul_rn(t, t);
+    if (pm < q3) return;
+    // getSqrRpSqrPi (source/device.cu:65-68).
+    const double pi1 = __ddiv_rn(q1, sqrL), pi2 = __ddiv_rn(q2, sqrL), pi3 = __ddiv_rn(q3, sqrL);
+    const double rp1 = __dsub_rn(abj.x, pi1), rp2 = __dsub_rn(abl.x, pi2), rp3 = __dsub_rn(s3, pi3);
+    if (!(rp1 < g.sqr_rpmax && rp2 < g.sqr_rpmax && rp3 < g.sqr_rpmax && rp1 > g.sqr_rpmin &&
+          rp2 > g.sqr_rpmin && rp3 > g.sqr_rpmin && pi1 < g.sqr_pimax && pi2 < g.sqr_pimax))
+      return;
+    idx = rppi_index(rp1, rp2, rp3, pi1, pi2, pi3, sb, g.nb, g.npi);
+    if (WEIGHTED) w = __dmul_rn(__dmul_rn(p1.w, pj.w), pl.w);
+  }
+  rppi_count<SURVEY, SYM, WEIGHTED>(a, idx, idx2, w, w2);
+}
+
+// Next pair of a lane after its flattened position moved on: rows j of the
+// pairs j < l < n (TRI), or of all (j, l) in n2 x n3.
+template <bool TRI>
+__device__ __forceinline__ void rppi_norm(int& j, int& l, int n2, int n3) {
+  if (TRI) {
+    while (l >= n2 && j < n2 - 1) {
+      ++j;
+      l += j + 1 - n2;
+    }
+  } else {
+    while (l >= n3 && j < n2) {
+      l -= n3;
+      ++j;
     }
   }
 }
@@ -189,195 +438,117 @@ template <bool SURVEY, bool SYM, bool WEIGHTED>
 __global__ void __launch_bounds__(kRppiThreads) k_rppi(const __grid_constant__ RppiArgs a) {
   const RppiGeom& g = a.g;
   __shared__ double s_sb[kMaxEdges];
-  __shared__ int s_off2[28], s_off3[28], s_cell[27];
-  __shared__ double s_sh[27][3];
   __shared__ float s_e2lo[kMaxEdges], s_e2hi[kMaxEdges];
-  __shared__ int s_anchor, s_n2, s_n3;
+  __shared__ RppiWarpSm s_w[kRppiWarps];
   for (int i = threadIdx.x; i <= g.nb; i += blockDim.x) {
     s_sb[i] = g.sqr_bins[i];
     s_e2lo[i] = g.fe2lo[i];
     s_e2hi[i] = g.fe2hi[i];
   }
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  double4_16a* pos2 = a.l_pos + static_cast<size_t>(blockIdx.x) * 2 * a.cap;
-  double4_16a* pos3 = SYM ? pos2 : pos2 + a.cap;
-  double2* ab2 = a.l_ab + static_cast<size_t>(blockIdx.x) * 2 * a.cap;
-  double2* ab3 = SYM ? ab2 : ab2 + a.cap;
-  float4* rel2 = a.l_rel + static_cast<size_t>(blockIdx.x) * 2 * a.cap;
-  float4* rel3 = SYM ? rel2 : rel2 + a.cap;
-  unsigned* meta2 = a.l_meta + static_cast<size_t>(blockIdx.x) * 2 * a.cap;
-  unsigned* meta3 = SYM ? meta2 : meta2 + a.cap;
-  unsigned long long n_exact = 0, n_fast = 0;
-  for (;;) {
-    __syncthreads();  // the previous anchor's lists are no longer read
-    if (threadIdx.x == 0) {
-      s_anchor = atomicAdd(a.work, 1);
-      s_n2 = 0;
-      s_n3 = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned lt = (1u << lane) - 1u;
+  RppiWarpSm& ws = s_w[warp];
+  const size_t wl0 = (static_cast<size_t>(blockIdx.x) * kRppiWarps + warp) * (SYM ? 1 : 2) * a.cap;
+  const size_t wl1 = SYM ? wl0 : wl0 + a.cap;
+  const RppiList L2 = {a.l_pos + wl0, a.l_ab + wl0, a.l_rel + wl0, a.l_meta + wl0, WEIGHTED ? a.l_pw + wl0 : nullptr};
+  const RppiList L3 = {a.l_pos + wl1, a.l_ab + wl1, a.l_rel + wl1, a.l_meta + wl1, WEIGHTED ? a.l_pw + wl1 : nullptr};
+  unsigned long long n_anchor = 0, n_scan = 0, n_pairs = 0, n_exact = 0, n_fast = 0;
+  bool overflow = false;
+  int cell = -1, excl2 = 0x7fffffff, excl3 = 0x7fffffff, tot2 = 0, tot3 = 0;
+  for (int ai = 0, last = 0;; ++ai) {
+    if (ai >= last) {
+      int first = 0;
+      if (lane == 0) first = atomicAdd(a.work, kRppiChunk);
+      first = __shfl_sync(kRppiFull, first, 0);
+      if (first >= a.n1) break;
+      ai = first;
+      last = min(first + kRppiChunk, a.n1);
     }
-    __syncthreads();
-    const int ai = s_anchor;
-    if (ai >= a.n1) break;
     const double4_16a p1 = a.a_pd[ai];
-    // Anchor cell (initCellIndexBox / initCellIndexSurvey, source/device.cu:75-87)
-    // and its 27 slots (shiftCellIndexBox / Survey, :89-153) in the
-    // reference's i, j, k order.
-    if (threadIdx.x < 27) {
-      const int s = threadIdx.x;
-      const double c3[3] = {p1.x, p1.y, p1.z};
-      const int sd[3] = {s / 9 - 1, (s / 3) % 3 - 1, s % 3 - 1};
-      int c[3];
-      bool ok = true;
-      for (int d = 0; d < 3; ++d) {
-        int h = static_cast<int>(__ddiv_rn(c3[d], g.cell[d]));
-        if (!SURVEY && h == g.nc[d]) --h;
-        c[d] = h + sd[d];
-        s_sh[s][d] = 0.0;
-        if (SURVEY) {
-          if (c[d] == g.nc[d] || c[d] == -1) ok = false;
-        } else if (c[d] == g.nc[d]) {
-          c[d] = 0;
-          s_sh[s][d] = g.box[d];
-        } else if (c[d] == -1) {
-          c[d] = g.nc[d] - 1;
-          s_sh[s][d] = -g.box[d];
-        }
-      }
-      const int cell = ok ? c[2] + g.nc[2] * (c[1] + g.nc[1] * c[0]) : -1;
-      s_cell[s] = cell < 0 ? 0 : cell;
-      s_off2[s + 1] = cell < 0 ? 0 : a.count2[cell];
-      s_off3[s + 1] = cell < 0 ? 0 : a.count3[cell];
+    const float4 p1f = a.a_pq[ai];
+    const int hc = __float_as_int(p1f.w);
+    if (hc != cell) {
+      cell = hc;
+      tot2 = rppi_slots<SURVEY>(g, hc, a.count2, a.start2, ws.s2, lane, excl2);
+      if (!SYM) tot3 = rppi_slots<SURVEY>(g, hc, a.count3, a.start3, ws.s3, lane, excl3);
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      s_off2[0] = 0;
-      s_off3[0] = 0;
-      for (int s = 0; s < 27; ++s) {
-        s_off2[s + 1] += s_off2[s];
-        s_off3[s + 1] += s_off3[s];
-      }
-    }
-    __syncthreads();
-    rppi_gather(a, p1, a.pd2, a.start2, s_off2, s_cell, s_sh, s_off2[27], &s_n2, pos2, ab2, rel2, meta2, s_sb,
-                a.cap);
+    int n2 = rppi_gather<SURVEY, WEIGHTED>(a, p1, p1f, a.pd2, a.pq2, ws.s2, excl2, tot2, ws.ring, L2, s_sb, lane,
+                                           overflow);
+    int n3 = n2;
     if (!SYM)
-      rppi_gather(a, p1, a.pd3, a.start3, s_off3, s_cell, s_sh, s_off3[27], &s_n3, pos3, ab3, rel3, meta3, s_sb,
-                  a.cap);
-    __syncthreads();
-    const int n2 = min(s_n2, a.cap);
-    const int n3 = SYM ? n2 : min(s_n3, a.cap);
-    if (threadIdx.x == 0) {
-      atomicAdd(&a.stats[0], 1ull);
-      atomicAdd(&a.stats[1], static_cast<unsigned long long>(s_off2[27] + (SYM ? 0 : s_off3[27])));
-      const unsigned long long pairs = (SYM && !SURVEY) ? static_cast<unsigned long long>(n2) * (n2 - 1) / 2
-                                                        : static_cast<unsigned long long>(n2) * n3;
-      atomicAdd(&a.stats[2], pairs);
-    }
+      n3 = rppi_gather<SURVEY, WEIGHTED>(a, p1, p1f, a.pd3, a.pq3, ws.s3, excl3, tot3, ws.ring, L3, s_sb, lane,
+                                         overflow);
+    n2 = min(n2, a.cap);
+    n3 = min(n3, a.cap);
+    ++n_anchor;
+    n_scan += static_cast<unsigned long long>(tot2 + (SYM ? 0 : tot3));
+    n_pairs += (SYM && !SURVEY) ? static_cast<unsigned long long>(n2) * (n2 - 1) / 2
+                                : static_cast<unsigned long long>(n2) * n3;
+    __syncwarp();  // the lists are complete
     // Phase B.
     double o1x = 0.0;
     if (SURVEY) o1x = __dsub_rn(p1.x, g.ori_x);  // pos1 = p1 - d_ori, d_ori = (ori.x, 0, 0)
-    for (int j = warp; j < n2; j += nwarps) {
-      const double4_16a pj = pos2[j];
-      const double2 abj = ab2[j];
-      const float4 rj = rel2[j];
-      const unsigned mj = SURVEY ? 0u : meta2[j];
-      const int l0 = (SYM && !SURVEY) ? j + 1 : 0;
-      for (int l = l0 + lane; l < n3; l += 32) {
-        if (SYM && l == j) continue;
-        const float4 rl = rel3[l];
-        const float dxf = rj.x - rl.x, dyf = rj.y - rl.y, dzf = rj.z - rl.z;
-        long long idx = -1, idx2 = -1;
-        double w = 1.0, w2 = 1.0;
+    constexpr bool kTri = SYM && !SURVEY;  // pairs j < l
+    int j = 0, l = kTri ? 1 + lane : lane;
+    rppi_norm<kTri>(j, l, n2, n3);
+    int head = 0, tail = 0;
+    for (;;) {
+      const bool valid = kTri ? j < n2 - 1 : j < n2;
+      if (!__any_sync(kRppiFull, valid)) break;
+      bool unc = false;
+      if (valid && !(SYM && SURVEY && j == l)) {
+        const float4 rj = L2.rel[j], rl = L3.rel[l];
         if (!SURVEY) {
-          if (dzf * dzf > g.f_pi_hi) continue;
-          const float rpf = fmaf(dxf, dxf, dyf * dyf);
-          if (rpf > g.f_rp_hi || rpf < g.f_rp_lo) continue;
-          // FP32 classification; the FP64 restatement below settles what it
+          // FP32 classification; the FP64 restatement settles what it
           // leaves uncertain.
-          const long long fi = rppi_fast_index(rj.x, rj.y, rj.z, rj.w, mj, rl.x, rl.y, rl.z, rl.w, meta3[l], g.fast,
-                                               s_e2lo, s_e2hi);
-          if (fi == -1) continue;
+          const long long fi = rppi_fast_index(rj.x, rj.y, rj.z, rj.w, L2.meta[j], rl.x, rl.y, rl.z, rl.w,
+                                               L3.meta[l], g.fast, s_e2lo, s_e2hi);
           if (fi >= 0) {
             ++n_fast;
-            idx = fi;
-            idx2 = fi;  // no rp^2 ties when the classifier is certain
+            double w = 1.0, w2 = 1.0;
             if (WEIGHTED) {
-              const double wl = pos3[l].w;
-              w = __dmul_rn(__dmul_rn(p1.w, pj.w), wl);
-              w2 = __dmul_rn(__dmul_rn(p1.w, wl), pj.w);
+              w = __dmul_rn(L2.pw[j], L3.pos[l].w);   // (w1 w2) w3
+              w2 = __dmul_rn(L3.pw[l], L2.pos[j].w);  // (w1 w3) w2
             }
+            rppi_count<SURVEY, SYM, WEIGHTED>(a, fi, fi, w, w2);  // no rp^2 ties when certain
           } else {
-            ++n_exact;
-            const double4_16a pl = pos3[l];
-            const double dz = __dsub_rn(pj.z, pl.z);
-            const double pi3 = __dmul_rn(dz, dz);
-            if (!(pi3 < g.sqr_pimax)) continue;
-            const double rp3 = rp_exact(__dsub_rn(pj.x, pl.x), __dsub_rn(pj.y, pl.y), g.rp_pattern);
-            if (!(rp3 < g.sqr_rpmax && rp3 > g.sqr_rpmin)) continue;
-            const double2 abl = ab3[l];
-            idx = rppi_index(abj.x, abl.x, rp3, abj.y, abl.y, pi3, s_sb, g.nb, g.npi);
-            if (idx < 0) continue;
-            if (WEIGHTED) w = __dmul_rn(__dmul_rn(p1.w, pj.w), pl.w);
-            if (SYM) {
-              // The (l, j) ordering: same sides, anchor sides swapped.
-              if (abj.x == abl.x || abj.x == rp3 || abl.x == rp3)
-                idx2 = rppi_index(abl.x, abj.x, rp3, abl.y, abj.y, pi3, s_sb, g.nb, g.npi);
-              else
-                idx2 = idx;
-              if (WEIGHTED) w2 = __dmul_rn(__dmul_rn(p1.w, pl.w), pj.w);
-            }
+            unc = fi == kRppiUncertain;
           }
         } else {
-          if (fmaf(dzf, dzf, fmaf(dxf, dxf, dyf * dyf)) > g.f_s_hi) continue;
-          ++n_exact;
-          const double4_16a pl = pos3[l];
-          const double s3 = sqr_sep_exact(pj.x, pj.y, pj.z, pl.x, pl.y, pl.z, g.fma_pattern);
-          if (!(s3 < g.sqr_rmax && s3 > g.sqr_rmin)) continue;
-          // getLOS (source/device.cu:45-56): positions relative to d_ori,
-          // summed left to right.
-          const double lx = __dadd_rn(__dadd_rn(o1x, __dsub_rn(pj.x, g.ori_x)), __dsub_rn(pl.x, g.ori_x));
-          const double ly = __dadd_rn(__dadd_rn(p1.y, pj.y), pl.y);
-          const double lz = __dadd_rn(__dadd_rn(p1.z, pj.z), pl.z);
-          const double sqrL = dot3_exact(lx, ly, lz, lx, ly, lz, g.dot_pattern);
-          const double pm = __dmul_rn(g.sqr_pimax, sqrL);
-          // getSqrSdotL (source/device.cu:58-63) for (p1,p2), (p1,p3), (p2,p3).
-          double t = dot3_exact(lx, ly, lz, __dsub_rn(p1.x, pj.x), __dsub_rn(p1.y, pj.y), __dsub_rn(p1.z, pj.z),
-                                g.dot_pattern);
-          const double q1 = __dmul_rn(t, t);
-          if (pm < q1) continue;
-          t = dot3_exact(lx, ly, lz, __dsub_rn(p1.x, pl.x), __dsub_rn(p1.y, pl.y), __dsub_rn(p1.z, pl.z),
-                         g.dot_pattern);
-          const double q2 = __dmul_rn(t, t);
-          if (pm < q2) continue;
-          t = dot3_exact(lx, ly, lz, __dsub_rn(pj.x, pl.x), __dsub_rn(pj.y, pl.y), __dsub_rn(pj.z, pl.z),
-                         g.dot_pattern);
-          const double q3 = __dmul_rn(t, t);
-          if (pm < q3) continue;
-          // getSqrRpSqrPi (source/device.cu:65-68).
-          const double pi1 = __ddiv_rn(q1, sqrL), pi2 = __ddiv_rn(q2, sqrL), pi3 = __ddiv_rn(q3, sqrL);
-          const double2 abl = ab3[l];
-          const double rp1 = __dsub_rn(abj.x, pi1), rp2 = __dsub_rn(abl.x, pi2), rp3 = __dsub_rn(s3, pi3);
-          if (!(rp1 < g.sqr_rpmax && rp2 < g.sqr_rpmax && rp3 < g.sqr_rpmax && rp1 > g.sqr_rpmin &&
-                rp2 > g.sqr_rpmin && rp3 > g.sqr_rpmin && pi1 < g.sqr_pimax && pi2 < g.sqr_pimax))
-            continue;
-          idx = rppi_index(rp1, rp2, rp3, pi1, pi2, pi3, s_sb, g.nb, g.npi);
-          if (WEIGHTED) w = __dmul_rn(__dmul_rn(p1.w, pj.w), pl.w);
-        }
-        if (SYM && !SURVEY) {
-          if (idx2 == idx && !WEIGHTED) {
-            rppi_add<false>(a, idx, 0.0, 2ull);
-          } else {
-            rppi_add<WEIGHTED>(a, idx, w, 1ull);
-            rppi_add<WEIGHTED>(a, idx2, w2, 1ull);
-          }
-        } else {
-          rppi_add<WEIGHTED>(a, idx, w, 1ull);
+          const float dxf = rj.x - rl.x, dyf = rj.y - rl.y, dzf = rj.z - rl.z;
+          unc = fmaf(dzf, dzf, fmaf(dxf, dxf, dyf * dyf)) <= g.f_s_hi;
         }
       }
+      const unsigned m = __ballot_sync(kRppiFull, unc);
+      if (unc) ws.ring[(tail + __popc(m & lt)) & (kRppiRing - 1)] = make_int2(j, l);
+      tail += __popc(m);
+      if (tail - head >= 32) {
+        __syncwarp();
+        rppi_exact_pair<SURVEY, SYM, WEIGHTED>(a, p1, o1x, ws.ring[(head + lane) & (kRppiRing - 1)], L2, L3, s_sb);
+        head += 32;
+        __syncwarp();
+      }
+      l += 32;
+      rppi_norm<kTri>(j, l, n2, n3);
     }
+    if (tail > head) {
+      __syncwarp();
+      if (lane < tail - head)
+        rppi_exact_pair<SURVEY, SYM, WEIGHTED>(a, p1, o1x, ws.ring[(head + lane) & (kRppiRing - 1)], L2, L3, s_sb);
+    }
+    n_exact += static_cast<unsigned long long>(tail);
+    __syncwarp();  // the ring and the lists are no longer read
   }
-  if (n_exact) atomicAdd(&a.stats[3], n_exact);
-  if (n_fast) atomicAdd(&a.stats[4], n_fast);
+  if (__any_sync(kRppiFull, overflow) && lane == 0) atomicOr(a.flags, kFlagListOverflow);
+  for (int o = 16; o; o >>= 1) n_fast += __shfl_xor_sync(kRppiFull, n_fast, o);
+  if (lane == 0 && n_anchor) {
+    atomicAdd(&a.stats[0], n_anchor);
+    atomicAdd(&a.stats[1], n_scan);
+    atomicAdd(&a.stats[2], n_pairs);
+    atomicAdd(&a.stats[3], n_exact);
+    atomicAdd(&a.stats[4], n_fast);
+  }
 }
 
 template <bool SURVEY, bool SYM, bool WEIGHTED>
@@ -473,6 +644,33 @@ int rppi_init(ncorr_handle* h, const double box[3], const double* edges, int n_e
   g.f_rp_lo = rpmin > 2.0 * slack ? f32_down((rpmin - 2.0 * slack) * (rpmin - 2.0 * slack)) : 0.0f;
   const double smax = std::sqrt(g.sqr_rmax);
   g.f_s_hi = f32_up((smax + 2.0 * slack) * (smax + 2.0 * slack));
+  // Gather prefilter. A valid point has |coordinate| < X = (nc + 1) cell per
+  // axis, and box <= nc cell. The FP32 offset of a neighbour in a box is
+  // fl(fl(fl(q) + fl(shift)) - fl(p1)), within u (5 X + |D|) of the true
+  // offset D (u = 2^-24, |D| < 2 cells); in a survey fl(fl(q) - fl(p1)),
+  // within u (2 X + |D|). The reference's own FP64 offset lies within
+  // 2^-50 X of D. With E the per-axis bound, the FP32 rp (pi, s) estimate is
+  // within |E_xy| (E_z, |E|) of the reference's, and the FP32 squares err by
+  // at most (1 + u)^2 (1 + u, (1 + u)^3) relatively; each threshold below adds
+  // those, plus a relative 2^-40 that covers the reference's FP64 rounding of
+  // the squares, so an estimate past it proves the reference cuts the point.
+  {
+    const double u = std::ldexp(1.0, -24);
+    double e[3];
+    for (int d = 0; d < 3; ++d) {
+      const double X = (g.nc[d] + 1.0) * g.cell[d];
+      e[d] = u * ((is_survey ? 2.0 : 5.0) * X + 2.0 * g.cell[d]) * (1.0 + 1e-6) + std::ldexp(X, -50);
+      g.fbox[d] = static_cast<float>(box[d]);
+    }
+    const double r40 = std::ldexp(1.0, -40);
+    const double er = std::sqrt(e[0] * e[0] + e[1] * e[1]) + rpmax * r40;
+    const double ez = e[2] + pimax * r40;
+    const double es = std::sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]) + smax * r40;
+    g.a_rp_hi = f32_up((rpmax + er) * (rpmax + er) * (1.0 + u) * (1.0 + u) * (1.0 + r40));
+    g.a_rp_lo = rpmin > er ? f32_down((rpmin - er) * (rpmin - er) * (1.0 - u) * (1.0 - u) * (1.0 - r40)) : -1.0f;
+    g.a_pi_hi = f32_up((pimax + ez) * (pimax + ez) * (1.0 + u) * (1.0 + r40));
+    g.a_s_hi = f32_up((smax + es) * (smax + es) * (1.0 + u) * (1.0 + u) * (1.0 + u) * (1.0 + r40));
+  }
   // The box-mode FP32 classifier: its bands and margins, derived in
   // rppi_fast.cuh (u = 2^-24).
   const double u = std::ldexp(1.0, -24);
@@ -532,6 +730,7 @@ static int rppi_grid_catalog(ncorr_handle* h, int ci, const double4_16a* d_in, i
   CU(c.start.ensure((h->ncell + 1) * sizeof(int)));
   CU(c.cursor.ensure(h->ncell * sizeof(int)));
   CU(c.pd.ensure(nn * sizeof(double4_16a)));
+  CU(c.pq.ensure(nn * sizeof(float4)));
   CU(cudaMemsetAsync(c.count.p, 0, h->ncell * sizeof(int), st));
   if (n > 0)
     k_rp_assign<<<(n + 255) / 256, 256, 0, st>>>(d_in, n, h->rg, c.cid.as<int>(), c.count.as<int>(),
@@ -539,7 +738,7 @@ static int rppi_grid_catalog(ncorr_handle* h, int ci, const double4_16a* d_in, i
   launch_scan(c.count.as<int>(), static_cast<int>(h->ncell), c.start.as<int>(), c.cursor.as<int>(), st);
   if (n > 0)
     k_rp_scatter<<<(n + 255) / 256, 256, 0, st>>>(d_in, n, c.cid.as<int>(), c.cursor.as<int>(),
-                                                  c.pd.as<double4_16a>());
+                                                  c.pd.as<double4_16a>(), c.pq.as<float4>());
   CU(cudaGetLastError());
   return NCORR_OK;
 }
@@ -611,12 +810,15 @@ int rppi_run(ncorr_handle* h, const double4_16a* d1, int n1, const double4_16a* 
   if (occ <= 0) return fail(NCORR_ERR_CUDA, "rppi kernel does not fit on the device");
   int nsm = 0;
   CU(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->device));
-  const int grid = std::max(1, std::min(n1, nsm * occ));
-  const size_t slab_n = static_cast<size_t>(grid) * 2 * cap;
+  // Warps take kRppiChunk anchors at a time: no more CTAs than that needs.
+  const long per_cta = static_cast<long>(kRppiWarps) * kRppiChunk;
+  const int grid = static_cast<int>(std::max(1L, std::min((n1 + per_cta - 1) / per_cta, static_cast<long>(nsm) * occ)));
+  const size_t slab_n = static_cast<size_t>(grid) * kRppiWarps * (sym ? 1 : 2) * cap;
   CU(h->rp_pos.ensure(slab_n * sizeof(double4_16a)));
   CU(h->rp_ab.ensure(slab_n * sizeof(double2)));
   CU(h->rp_rel.ensure(slab_n * sizeof(float4)));
   CU(h->rp_meta.ensure(slab_n * sizeof(unsigned)));
+  if (weighted) CU(h->rp_pw.ensure(slab_n * sizeof(double)));
   const size_t hist_n = static_cast<size_t>(g.nbins) + 1;
   CU(h->d_hist.ensure(hist_n * sizeof(double)));
   CU(cudaMemsetAsync(h->d_hist.p, 0, hist_n * sizeof(double), st));
@@ -625,17 +827,21 @@ int rppi_run(ncorr_handle* h, const double4_16a* d1, int n1, const double4_16a* 
   std::memset(&a, 0, sizeof(a));
   a.g = g;
   a.a_pd = h->cat[role[0]].pd.as<double4_16a>();
+  a.a_pq = h->cat[role[0]].pq.as<float4>();
   a.n1 = n1;
   a.pd2 = h->cat[role[1]].pd.as<double4_16a>();
+  a.pq2 = h->cat[role[1]].pq.as<float4>();
   a.start2 = h->cat[role[1]].start.as<int>();
   a.count2 = h->cat[role[1]].count.as<int>();
   a.pd3 = h->cat[role[2]].pd.as<double4_16a>();
+  a.pq3 = h->cat[role[2]].pq.as<float4>();
   a.start3 = h->cat[role[2]].start.as<int>();
   a.count3 = h->cat[role[2]].count.as<int>();
   a.l_pos = h->rp_pos.as<double4_16a>();
   a.l_ab = h->rp_ab.as<double2>();
   a.l_rel = h->rp_rel.as<float4>();
   a.l_meta = h->rp_meta.as<unsigned>();
+  a.l_pw = weighted ? h->rp_pw.as<double>() : nullptr;
   a.cap = cap;
   a.hist_u = weighted ? nullptr : h->d_hist.as<unsigned long long>();
   a.hist_w = weighted ? h->d_hist.as<double>() : nullptr;

@@ -31,6 +31,14 @@ struct RppiGeom {
   float f_rp_hi;     // box: rp^2 estimate > f_rp_hi  => rp^2 >= rpMax^2
   float f_rp_lo;     // box: rp^2 estimate < f_rp_lo  => rp^2 <= rpMin^2
   float f_s_hi;      // survey: s^2 estimate > f_s_hi => s^2 >= sqrRMax
+  // FP32 prefilter of the neighbour gather, on the points' FP32 copies (each
+  // coordinate rounded once) and FP32 image shifts: a point whose estimate
+  // passes one of these thresholds is certainly cut against the anchor.
+  float fbox[3];     // fl32(box)
+  float a_pi_hi;     // box: dz^2 estimate > a_pi_hi  => pi^2 >= piMax^2
+  float a_rp_hi;     // box: rp^2 estimate > a_rp_hi  => rp^2 >= rpMax^2
+  float a_rp_lo;     // box: rp^2 estimate < a_rp_lo  => rp^2 <= rpMin^2 (-1: never)
+  float a_s_hi;      // survey: s^2 estimate > a_s_hi => s^2 >= sqrRMax
   long long nbins;   // nb^3 * nPi^2
   // Box mode: the FP32 classifier (rppi_fast.cuh) and its bin-edge bounds.
   RppiFast fast;
@@ -41,18 +49,23 @@ struct RppiGeom {
 struct RppiArgs {
   RppiGeom g;
   const double4_16a* a_pd;  // anchors (cell order)
+  const float4* a_pq;       // their FP32 copies; .w = cell id (int bits)
   int n1;
   const double4_16a* pd2;
+  const float4* pq2;
   const int* start2;
   const int* count2;
   const double4_16a* pd3;
+  const float4* pq3;
   const int* start3;
   const int* count3;
-  // Per-CTA neighbour lists (two lists of `cap` entries per CTA).
+  // Per-warp neighbour lists: one list of `cap` entries per warp when p2 and
+  // p3 are one catalogue, two otherwise.
   double4_16a* l_pos;  // neighbour (its image in a box), weight
   double2* l_ab;       // box: (rp^2, pi^2) to the anchor; survey: (sqrS, 0)
   float4* l_rel;       // FP32 anchor-relative offset; box: .w = sqrt_rn(fl32(rp^2))
   unsigned* l_meta;    // box: exact rp bin | pi bin << 16 of the anchor side
+  double* l_pw;        // weighted: fl(w_anchor * w_neighbour); else null
   int cap;
   unsigned long long* hist_u;  // nbins + 1 counts; [nbins] collects indices past the end
   double* hist_w;              // nbins + 1 weighted sums (same layout)
