@@ -502,7 +502,7 @@ __global__ void __launch_bounds__(kRppiThreads) k_rppi(const __grid_constant__ R
         if (!SURVEY) {
           // FP32 classification; the FP64 restatement settles what it
           // leaves uncertain.
-          const long long fi = rppi_fast_index(rj.x, rj.y, rj.z, rj.w, L2.meta[j], rl.x, rl.y, rl.z, rl.w,
+          const int fi = rppi_fast_index(rj.x, rj.y, rj.z, rj.w, L2.meta[j], rl.x, rl.y, rl.z, rl.w,
                                                L3.meta[l], g.fast, s_e2lo, s_e2hi);
           if (fi >= 0) {
             ++n_fast;
@@ -686,6 +686,7 @@ int rppi_init(ncorr_handle* h, const double box[3], const double* edges, int n_e
   f.pmarg = f32_up(16.0 * u * g.sqr_pimax);
   f.nb = nb;
   f.npi = num_minor_bins;
+  f.step0 = rppi_step0(nb);
   for (int i = 0; i < n_edges; ++i) {
     g.fe2lo[i] = f32_down(g.sqr_bins[i]);
     g.fe2hi[i] = f32_up(g.sqr_bins[i]);

@@ -40,71 +40,85 @@ struct RppiFast {
   float hm;                    // -M of the triangle margin
   float pmarg;                 // pi-bin margin
   int nb, npi;
+  int step0;                   // largest power of two <= nb - 1 (0 when nb == 1)
 };
 
-constexpr long long kRppiUncertain = -2;
+constexpr int kRppiUncertain = -2;
 
-// The flat index, -1 (the reference certainly does not count it), or
-// kRppiUncertain. e2lo/e2hi: FP32 neighbours below / above each bin edge^2.
-__host__ __device__ inline long long rppi_fast_index(float xj, float yj, float zj, float rj, unsigned mj, float xl,
-                                                     float yl, float zl, float rl, unsigned ml, const RppiFast& f,
-                                                     const float* e2lo, const float* e2hi) {
+inline int rppi_step0(int nb) {
+  int s = 0;
+  if (nb > 1) {
+    s = 1;
+    while (2 * s <= nb - 1) s *= 2;
+  }
+  return s;
+}
+
+// An estimate of sqrt(x) for x >= 0; its error only costs certainty (the
+// pi-bin test below checks the bin it gives against margins).
+__host__ __device__ inline float rppi_sqrt_est(float x) {
+#ifdef __CUDA_ARCH__
+  float r;
+  asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+#else
+  return std::sqrt(x);
+#endif
+}
+
+// The flat index (below 2^31: the constructor checks nb^3 nPi^2 + nPi), -1
+// (the reference certainly does not count it), or kRppiUncertain.
+// e2lo/e2hi: FP32 neighbours below / above each bin edge^2, nb + 1 entries.
+// Every test is evaluated and combined with selects (no early return), so a
+// warp classifying 32 pairs runs a single path.
+__host__ __device__ inline int rppi_fast_index(float xj, float yj, float zj, float rj, unsigned mj, float xl,
+                                               float yl, float zl, float rl, unsigned ml, const RppiFast& f,
+                                               const float* e2lo, const float* e2hi) {
   const float dz = zj - zl, dx = xj - xl, dy = yj - yl;
   const float pf = dz * dz;
-  if (!(pf + f.epi < f.pimax2)) return (pf - f.epi >= f.pimax2) ? -1 : kRppiUncertain;
   const float rf = fmaf(dx, dx, dy * dy);
   const float lo = rf - f.erp, hi = rf + f.erp;
-  if (lo >= f.rpmax2_hi || hi < f.rpmin2_lo) return -1;
-  if (!(lo > f.rpmin2_hi && hi < f.rpmax2_lo)) return kRppiUncertain;
+  // Certainly cut: pi3 >= piMax^2, or rp3 outside (rpMin^2, rpMax^2).
+  const bool reject = pf - f.epi >= f.pimax2 || lo >= f.rpmax2_hi || hi < f.rpmin2_lo;
+  bool ok = pf + f.epi < f.pimax2 && lo > f.rpmin2_hi && hi < f.rpmax2_lo;
   // Order of the three rp^2: rho is monotone in rp^2, so rho_j < rho_l
   // proves A < B; equal rho leaves the order open.
-  if (rj == rl) return kRppiUncertain;
+  ok = ok && rj != rl;
   const bool jfirst = rj < rl;
   const float a = rj * rj, b = rl * rl;
   const float mn = jfirst ? a : b, mx = jfirst ? b : a;
-  int pos;  // anchor sides below rp3
-  if (hi < mn)
-    pos = 0;
-  else if (lo > mx)
-    pos = 2;
-  else if (lo > mn && hi < mx)
-    pos = 1;
-  else
-    return kRppiUncertain;
+  const bool below = hi < mn, above = lo > mx, between = lo > mn && hi < mx;
+  ok = ok && (below || above || between);
+  const int pos = below ? 0 : (above ? 2 : 1);  // anchor sides below rp3
   // Triangle test.
   const float p = -2.0f * fmaf(xj, xl, yj * yl);
-  if (!(fabsf(p) < fmaf(2.0f * rj, rl, f.hm))) return kRppiUncertain;
-  // rp bin of the third side.
-  int b3 = 0, bh = f.nb - 1;
-  while (b3 < bh) {
-    const int mid = (b3 + bh + 1) >> 1;
-    if (rf >= e2lo[mid])
-      b3 = mid;
-    else
-      bh = mid - 1;
+  ok = ok && fabsf(p) < fmaf(2.0f * rj, rl, f.hm);
+  // rp bin of the third side: the largest b < nb with rf >= e2lo[b].
+  int b3 = 0;
+  for (int step = f.step0; step; step >>= 1) {
+    const int c = b3 + step;
+    const float e = e2lo[c < f.nb ? c : f.nb];
+    b3 = (c < f.nb && rf >= e) ? c : b3;
   }
-  if (!(lo > e2hi[b3] && hi < e2lo[b3 + 1])) return kRppiUncertain;
+  ok = ok && lo > e2hi[b3] && hi < e2lo[b3 + 1];
   // pi bin of the third side, needed when it is one of the two shortest.
-  int p3 = 0;
-  if (pos < 2) {
-    const int k = static_cast<int>(floorf(sqrtf(pf)));
-    const float k2 = static_cast<float>(k * k), k3 = static_cast<float>((k + 1) * (k + 1));
-    const float w = f.epi + f.pmarg;
-    if (!((k == 0 || pf - w > k2) && pf + w < k3)) return kRppiUncertain;
-    p3 = k;
-  }
-  const int rs = static_cast<int>((jfirst ? mj : ml) & 0xffffu), ps = static_cast<int>((jfirst ? mj : ml) >> 16);
-  const int rL = static_cast<int>((jfirst ? ml : mj) & 0xffffu), pL = static_cast<int>((jfirst ? ml : mj) >> 16);
-  int r1, r2, r3, q1, q2;  // sorted ascending: rp bins and pi bins of the two shortest
-  if (pos == 0) {
-    r1 = b3; q1 = p3; r2 = rs; q2 = ps; r3 = rL;
-  } else if (pos == 1) {
-    r1 = rs; q1 = ps; r2 = b3; q2 = p3; r3 = rL;
-  } else {
-    r1 = rs; q1 = ps; r2 = rL; q2 = pL; r3 = b3;
-  }
-  const long long P = f.npi, B = f.nb;
-  return q2 + q1 * P + r3 * P * P + r2 * B * P * P + static_cast<long long>(r1) * B * B * P * P;
+  const int k = static_cast<int>(fminf(rppi_sqrt_est(pf), 4095.0f));
+  const float k2 = static_cast<float>(k * k), k3 = static_cast<float>((k + 1) * (k + 1));
+  const float w = f.epi + f.pmarg;
+  ok = ok && (pos == 2 || ((k == 0 || pf - w > k2) && pf + w < k3));
+  const unsigned ms = jfirst ? mj : ml, mL = jfirst ? ml : mj;
+  const int rs = static_cast<int>(ms & 0xffffu), ps = static_cast<int>(ms >> 16);
+  const int rL = static_cast<int>(mL & 0xffffu), pL = static_cast<int>(mL >> 16);
+  // Sorted ascending: rp bins r1 <= r2 <= r3, pi bins q1, q2 of the two shortest.
+  const int r1 = pos == 0 ? b3 : rs;
+  const int q1 = pos == 0 ? k : ps;
+  const int r2 = pos == 0 ? rs : (pos == 1 ? b3 : rL);
+  const int q2 = pos == 0 ? ps : (pos == 1 ? k : pL);
+  const int r3 = pos == 2 ? b3 : rL;
+  // Unsigned: the discarded values of uncertain pairs may wrap.
+  const unsigned P = static_cast<unsigned>(f.npi), B = static_cast<unsigned>(f.nb);
+  const unsigned idx = q2 + P * (q1 + P * (r3 + B * (r2 + B * static_cast<unsigned>(r1))));
+  return reject ? -1 : (ok ? static_cast<int>(idx) : kRppiUncertain);
 }
 
 }  // namespace ncorr_gb300

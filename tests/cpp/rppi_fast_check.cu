@@ -94,6 +94,7 @@ int main(int argc, char** argv) {
   f.pmarg = f32_up(16.0 * kU * sqr_pimax);
   f.nb = nb;
   f.npi = npi;
+  f.step0 = ncorr_gb300::rppi_step0(nb);
   std::vector<float> e2lo(nb + 1), e2hi(nb + 1);
   for (int i = 0; i <= nb; ++i) {
     e2lo[i] = f32_down(sb[i]);
