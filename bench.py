@@ -153,9 +153,10 @@ def engine_launches(n_distinct: int, sym: bool, learned: bool = False, rppi: boo
     """Kernels one calculateD1D2D3 launches: per distinct catalogue the cell
     list (assign, scan, scatter), the neighbourhood bound per list catalogue,
     then the triangle kernel with its exact pass and fold (threeD) or the
-    rppi kernel; the learned schedule adds the features, the prediction and
-    seven queue-building kernels."""
-    n = 3 * n_distinct + (1 if sym else 2) + (1 if rppi else 3)
+    rppi kernel with the fold of its histogram copies (a histogram under
+    32 MiB has more than one); the learned schedule adds the features, the
+    prediction and seven queue-building kernels."""
+    n = 3 * n_distinct + (1 if sym else 2) + (2 if rppi else 3)
     return n + (9 if learned else 0)
 
 

@@ -454,7 +454,7 @@ void ncorr_destroy(ncorr_handle* h) {
   for (DevBuf* b : {&h->d_table, &h->d_flags, &h->d_wmax, &h->d_work, &h->d_bound, &h->d_hist,
                     &h->d_out, &h->d_stats, &h->d_total, &h->slab_e,
                     &h->slab_w, &h->slab_q, &h->slab_x, &h->cta_time, &h->xq, &h->xq_count, &h->d_args, &h->d_items, &h->d_cell_work,
-                    &h->d_feats, &h->q_item, &h->q_anchor, &h->rp_pos, &h->rp_ab, &h->rp_rel, &h->rp_meta, &h->rp_pw})
+                    &h->d_feats, &h->q_item, &h->q_anchor, &h->rp_pos, &h->rp_ab, &h->rp_rel, &h->rp_meta, &h->rp_pw, &h->rp_tab})
     b->release();
   h->order.release();
   for (auto& e : h->ev)

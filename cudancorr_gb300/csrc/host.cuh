@@ -167,11 +167,12 @@ struct ncorr_handle {
   ncorr_host::OrderBufs order;
   std::vector<float> rec_feats;   // features of the last recorded call, ncell x 28
   std::vector<double> rec_work;   // its candidate pairs per cell of catalogue 1
-  // rppi bin type: geometry, piBinsOut_ table (2 per entry), per-CTA lists,
+  // rppi bin type: geometry, piBinsOut_ table (2 per entry), per-warp lists,
   // weight of the last call's triangles indexed past triCountsAll_.
   ncorr_gb300::RppiGeom rg;
   std::vector<double> pi_bins_out;
-  ncorr_host::DevBuf rp_pos, rp_ab, rp_rel, rp_meta, rp_pw;
+  ncorr_host::DevBuf rp_pos, rp_ab, rp_rel, rp_meta, rp_pw, rp_tab;
+  std::vector<unsigned char> rp_tab_host;  // the box classifier's rp3 table
   double rppi_overflow = 0.0;
 };
 

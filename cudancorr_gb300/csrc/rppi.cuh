@@ -66,9 +66,11 @@ struct RppiArgs {
   float4* l_rel;       // FP32 anchor-relative offset; box: .w = sqrt_rn(fl32(rp^2))
   unsigned* l_meta;    // box: exact rp bin | pi bin << 16 of the anchor side
   double* l_pw;        // weighted: fl(w_anchor * w_neighbour); else null
+  const unsigned char* tab;  // box: the classifier's rp3 table (kRppiTab entries)
   int cap;
-  unsigned long long* hist_u;  // nbins + 1 counts; [nbins] collects indices past the end
-  double* hist_w;              // nbins + 1 weighted sums (same layout)
+  unsigned long long* hist_u;  // hist_copies x (nbins + 1) counts; [nbins] collects indices past the end
+  double* hist_w;              // the same for weighted sums
+  int hist_copies;             // CTA b adds to copy b % hist_copies
   int* work;
   int* flags;
   unsigned long long* stats;   // [0] anchors, [1] scanned, [2] candidate pairs, [3] FP64 evaluations,

@@ -39,19 +39,46 @@ struct RppiFast {
   float rpmin2_lo, rpmin2_hi;  // and rpMin^2
   float hm;                    // -M of the triangle margin
   float pmarg;                 // pi-bin margin
+  float tab_scale;             // 2^k: entry of the rp3 table for an estimate rf
   int nb, npi;
-  int step0;                   // largest power of two <= nb - 1 (0 when nb == 1)
 };
 
 constexpr int kRppiUncertain = -2;
 
-inline int rppi_step0(int nb) {
-  int s = 0;
-  if (nb > 1) {
-    s = 1;
-    while (2 * s <= nb - 1) s *= 2;
+// The rp3 table: kRppiTab entries over the estimate rf of the third side's
+// rp^2, entry c for rf in [c, c + 1) / tab_scale (the last one for everything
+// above). An entry holds the bin b when every rf of its cell has
+// rf - erp > fl32 up(edge_b^2) and rf + erp < fl32 down(edge_{b+1}^2): the
+// reference's rp3 (within erp of rf) then lies in bin b, and so within
+// (rpMin^2, rpMax^2). It holds kRppiTabReject when every rf of the cell has
+// rf - erp >= rpmax2_hi or rf + erp < rpmin2_lo (rp3 certainly cut), else
+// kRppiTabUncertain. The bounds are evaluated exactly (in FP64, from FP32
+// inputs), and tab_scale is a power of two, so the kernel's cell index
+// floor(rf * tab_scale) is exact.
+constexpr int kRppiTab = 1 << 14;
+constexpr unsigned char kRppiTabReject = 0xFE, kRppiTabUncertain = 0xFF;
+
+inline float rppi_tab_scale(float rpmax2_hi, float erp) {
+  // The largest power of two with (kRppiTab - 1) / scale >= rpmax2_hi + erp,
+  // so that the last (clamped) entry is a reject.
+  const double need = (static_cast<double>(rpmax2_hi) + erp) / (kRppiTab - 1);
+  return static_cast<float>(std::ldexp(1.0, -static_cast<int>(std::ceil(std::log2(need)))));
+}
+
+inline void rppi_build_table(const RppiFast& f, const float* e2lo, const float* e2hi, unsigned char* tab) {
+  const double inv = 1.0 / f.tab_scale;
+  for (int c = 0; c < kRppiTab; ++c) {
+    const double lo = c * inv - f.erp;  // infimum of rf - erp over the cell
+    const double hi = c == kRppiTab - 1 ? INFINITY : (c + 1) * inv + f.erp;  // supremum of rf + erp
+    unsigned char code = kRppiTabUncertain;
+    if (lo >= f.rpmax2_hi || hi <= f.rpmin2_lo) {
+      code = kRppiTabReject;
+    } else {
+      for (int b = 0; b < f.nb; ++b)
+        if (lo > e2hi[b] && hi <= e2lo[b + 1]) code = static_cast<unsigned char>(b);
+    }
+    tab[c] = code;
   }
-  return s;
 }
 
 // An estimate of sqrt(x) for x >= 0; its error only costs certainty (the
@@ -67,20 +94,21 @@ __host__ __device__ inline float rppi_sqrt_est(float x) {
 }
 
 // The flat index (below 2^31: the constructor checks nb^3 nPi^2 + nPi), -1
-// (the reference certainly does not count it), or kRppiUncertain.
-// e2lo/e2hi: FP32 neighbours below / above each bin edge^2, nb + 1 entries.
-// Every test is evaluated and combined with selects (no early return), so a
-// warp classifying 32 pairs runs a single path.
+// (the reference certainly does not count it), or kRppiUncertain. `tab` is
+// the rp3 table. Every test is evaluated and combined with selects (no early
+// return), so a warp classifying 32 pairs runs a single path.
 __host__ __device__ inline int rppi_fast_index(float xj, float yj, float zj, float rj, unsigned mj, float xl,
                                                float yl, float zl, float rl, unsigned ml, const RppiFast& f,
-                                               const float* e2lo, const float* e2hi) {
+                                               const unsigned char* tab) {
   const float dz = zj - zl, dx = xj - xl, dy = yj - yl;
   const float pf = dz * dz;
   const float rf = fmaf(dx, dx, dy * dy);
   const float lo = rf - f.erp, hi = rf + f.erp;
+  const int b3 = tab[static_cast<int>(fminf(rf * f.tab_scale, static_cast<float>(kRppiTab - 1)))];
   // Certainly cut: pi3 >= piMax^2, or rp3 outside (rpMin^2, rpMax^2).
-  const bool reject = pf - f.epi >= f.pimax2 || lo >= f.rpmax2_hi || hi < f.rpmin2_lo;
-  bool ok = pf + f.epi < f.pimax2 && lo > f.rpmin2_hi && hi < f.rpmax2_lo;
+  const bool reject = pf - f.epi >= f.pimax2 || b3 == kRppiTabReject;
+  // rp3 certainly in range and in bin b3; pi3 certainly below piMax^2.
+  bool ok = pf + f.epi < f.pimax2 && b3 < kRppiTabReject;
   // Order of the three rp^2: rho is monotone in rp^2, so rho_j < rho_l
   // proves A < B; equal rho leaves the order open.
   ok = ok && rj != rl;
@@ -93,14 +121,6 @@ __host__ __device__ inline int rppi_fast_index(float xj, float yj, float zj, flo
   // Triangle test.
   const float p = -2.0f * fmaf(xj, xl, yj * yl);
   ok = ok && fabsf(p) < fmaf(2.0f * rj, rl, f.hm);
-  // rp bin of the third side: the largest b < nb with rf >= e2lo[b].
-  int b3 = 0;
-  for (int step = f.step0; step; step >>= 1) {
-    const int c = b3 + step;
-    const float e = e2lo[c < f.nb ? c : f.nb];
-    b3 = (c < f.nb && rf >= e) ? c : b3;
-  }
-  ok = ok && lo > e2hi[b3] && hi < e2lo[b3 + 1];
   // pi bin of the third side, needed when it is one of the two shortest.
   const int k = static_cast<int>(fminf(rppi_sqrt_est(pf), 4095.0f));
   const float k2 = static_cast<float>(k * k), k3 = static_cast<float>((k + 1) * (k + 1));

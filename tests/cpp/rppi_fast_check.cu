@@ -94,12 +94,14 @@ int main(int argc, char** argv) {
   f.pmarg = f32_up(16.0 * kU * sqr_pimax);
   f.nb = nb;
   f.npi = npi;
-  f.step0 = ncorr_gb300::rppi_step0(nb);
   std::vector<float> e2lo(nb + 1), e2hi(nb + 1);
   for (int i = 0; i <= nb; ++i) {
     e2lo[i] = f32_down(sb[i]);
     e2hi[i] = f32_up(sb[i]);
   }
+  f.tab_scale = ncorr_gb300::rppi_tab_scale(f.rpmax2_hi, f.erp);
+  std::vector<unsigned char> tab(ncorr_gb300::kRppiTab);
+  ncorr_gb300::rppi_build_table(f, e2lo.data(), e2hi.data(), tab.data());
 
   std::mt19937_64 rng(seed);
   std::uniform_real_distribution<double> U(0.0, 1.0);
@@ -128,7 +130,7 @@ int main(int argc, char** argv) {
     const unsigned ml = static_cast<unsigned>(exact_bin(B, sb)) |
                         (static_cast<unsigned>(std::floor(std::sqrt(static_cast<float>(Pl)))) << 16);
     const long long got =
-        ncorr_gb300::rppi_fast_index(xj, yj, zj, rj, mj, xl, yl, zl, rl, ml, f, e2lo.data(), e2hi.data());
+        ncorr_gb300::rppi_fast_index(xj, yj, zj, rj, mj, xl, yl, zl, rl, ml, f, tab.data());
     if (got == ncorr_gb300::kRppiUncertain) return;
     ++certain;
     if (got >= 0) ++counted;
