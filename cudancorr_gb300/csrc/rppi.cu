@@ -538,8 +538,7 @@ __global__ void __launch_bounds__(kRppiThreads) k_rppi(const __grid_constant__ R
     int head = 0, tail = 0;
     const int nbins32 = static_cast<int>(g.nbins);  // below 2^31
     // Lanes past the end read entry 0 (the lists are not empty while a lane
-    // is valid) and discard the result. Each round loads the next round's
-    // entries before it classifies its own, so that their latency is hidden.
+    // is valid) and discard the result.
     bool valid = kTri ? j < n2 - 1 : j < n2;
     int jj = valid ? j : 0, ll = valid ? l : 0;
     float4 rj = L2.rel[jj], rl = L3.rel[ll];
@@ -547,9 +546,39 @@ __global__ void __launch_bounds__(kRppiThreads) k_rppi(const __grid_constant__ R
     for (;;) {
       if (!__any_sync(kRppiFull, valid)) break;
       const bool vc = (SYM && SURVEY) ? valid && j != l : valid;
-      const int jc = j, lc = l, jjc = jj, llc = ll;
-      const float4 rjc = rj, rlc = rl;
-      const unsigned mjc = mj, mlc = ml;
+      bool unc;
+      if (!SURVEY) {
+        // FP32 classification; the FP64 restatement settles what it leaves
+        // uncertain.
+        const int fi = rppi_fast_index(rj.x, rj.y, rj.z, rj.w, mj, rl.x, rl.y, rl.z, rl.w, ml, g.fast,
+                                       s_tab);
+        const bool hit = vc && fi >= 0;
+        n_fast += hit ? 1u : 0u;
+        if (WEIGHTED) {
+          if (hit) {
+            const double w = __dmul_rn(L2.pw[jj], L3.pos[ll].w);   // (w1 w2) w3
+            const double w2 = __dmul_rn(L3.pw[ll], L2.pos[jj].w);  // (w1 w3) w2
+            rppi_count<SURVEY, SYM, WEIGHTED>(out, fi, fi, w, w2);  // no rp^2 ties when certain
+          }
+        } else {
+          // One count per ordering (two when p2 == p3: no rp^2 ties when
+          // certain); indices past the histogram go to its overflow slot.
+          rppi_red_u64(hit, out.u + min(max(fi, 0), nbins32), SYM ? 2ull : 1ull);
+        }
+        unc = vc && fi == kRppiUncertain;
+      } else {
+        const float dxf = rj.x - rl.x, dyf = rj.y - rl.y, dzf = rj.z - rl.z;
+        unc = vc && fmaf(dzf, dzf, fmaf(dxf, dxf, dyf * dyf)) <= g.f_s_hi;
+      }
+      const unsigned m = __ballot_sync(kRppiFull, unc);
+      if (unc) ws.ring[(tail + __popc(m & lt)) & (kRppiRing - 1)] = make_int2(j, l);
+      tail += __popc(m);
+      if (tail - head >= 32) {
+        __syncwarp();
+        rppi_exact_pair<SURVEY, SYM, WEIGHTED>(a, out, p1, o1x, ws.ring[(head + lane) & (kRppiRing - 1)], L2, L3, s_sb);
+        head += 32;
+        __syncwarp();
+      }
       l += 32;
       rppi_norm<kTri>(j, l, n2, n3);
       valid = kTri ? j < n2 - 1 : j < n2;
@@ -560,39 +589,6 @@ __global__ void __launch_bounds__(kRppiThreads) k_rppi(const __grid_constant__ R
       if (!SURVEY) {
         mj = L2.meta[jj];
         ml = L3.meta[ll];
-      }
-      bool unc;
-      if (!SURVEY) {
-        // FP32 classification; the FP64 restatement settles what it leaves
-        // uncertain.
-        const int fi = rppi_fast_index(rjc.x, rjc.y, rjc.z, rjc.w, mjc, rlc.x, rlc.y, rlc.z, rlc.w, mlc, g.fast,
-                                       s_tab);
-        const bool hit = vc && fi >= 0;
-        n_fast += hit ? 1u : 0u;
-        if (WEIGHTED) {
-          if (hit) {
-            const double w = __dmul_rn(L2.pw[jjc], L3.pos[llc].w);   // (w1 w2) w3
-            const double w2 = __dmul_rn(L3.pw[llc], L2.pos[jjc].w);  // (w1 w3) w2
-            rppi_count<SURVEY, SYM, WEIGHTED>(out, fi, fi, w, w2);  // no rp^2 ties when certain
-          }
-        } else {
-          // One count per ordering (two when p2 == p3: no rp^2 ties when
-          // certain); indices past the histogram go to its overflow slot.
-          rppi_red_u64(hit, out.u + min(max(fi, 0), nbins32), SYM ? 2ull : 1ull);
-        }
-        unc = vc && fi == kRppiUncertain;
-      } else {
-        const float dxf = rjc.x - rlc.x, dyf = rjc.y - rlc.y, dzf = rjc.z - rlc.z;
-        unc = vc && fmaf(dzf, dzf, fmaf(dxf, dxf, dyf * dyf)) <= g.f_s_hi;
-      }
-      const unsigned m = __ballot_sync(kRppiFull, unc);
-      if (unc) ws.ring[(tail + __popc(m & lt)) & (kRppiRing - 1)] = make_int2(jc, lc);
-      tail += __popc(m);
-      if (tail - head >= 32) {
-        __syncwarp();
-        rppi_exact_pair<SURVEY, SYM, WEIGHTED>(a, out, p1, o1x, ws.ring[(head + lane) & (kRppiRing - 1)], L2, L3, s_sb);
-        head += 32;
-        __syncwarp();
       }
     }
     if (tail > head) {
@@ -616,7 +612,7 @@ __global__ void __launch_bounds__(kRppiThreads) k_rppi(const __grid_constant__ R
 
 // Sums the histogram copies (n bins each) into copy 0.
 template <bool WEIGHTED>
-__global__ void k_rppi_fold(unsigned long long* __restrict__ hu, double* __restrict__ hw, long long n, int copies) {
+__global__ void k_rp_fold(unsigned long long* __restrict__ hu, double* __restrict__ hw, long long n, int copies) {
   for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
        i += static_cast<long long>(gridDim.x) * blockDim.x) {
     if (WEIGHTED) {
@@ -950,9 +946,9 @@ int rppi_run(ncorr_handle* h, const double4_16a* d1, int n1, const double4_16a* 
   if (n1 > 0 && copies > 1) {
     const int fb = static_cast<int>(std::min<size_t>((hist_n + 255) / 256, static_cast<size_t>(nsm) * 8));
     if (weighted)
-      k_rppi_fold<true><<<fb, 256, 0, st>>>(nullptr, a.hist_w, static_cast<long long>(hist_n), copies);
+      k_rp_fold<true><<<fb, 256, 0, st>>>(nullptr, a.hist_w, static_cast<long long>(hist_n), copies);
     else
-      k_rppi_fold<false><<<fb, 256, 0, st>>>(a.hist_u, nullptr, static_cast<long long>(hist_n), copies);
+      k_rp_fold<false><<<fb, 256, 0, st>>>(a.hist_u, nullptr, static_cast<long long>(hist_n), copies);
     CU(cudaGetLastError());
   }
   CU(cudaEventRecord(h->ev[3], st));

@@ -105,27 +105,28 @@ __host__ __device__ inline int rppi_fast_index(float xj, float yj, float zj, flo
   const float rf = fmaf(dx, dx, dy * dy);
   const float lo = rf - f.erp, hi = rf + f.erp;
   const int b3 = tab[static_cast<int>(fminf(rf * f.tab_scale, static_cast<float>(kRppiTab - 1)))];
+  // The tests below combine with & and | (no short-circuit): one path.
   // Certainly cut: pi3 >= piMax^2, or rp3 outside (rpMin^2, rpMax^2).
-  const bool reject = pf - f.epi >= f.pimax2 || b3 == kRppiTabReject;
+  const bool reject = (pf - f.epi >= f.pimax2) | (b3 == kRppiTabReject);
   // rp3 certainly in range and in bin b3; pi3 certainly below piMax^2.
-  bool ok = pf + f.epi < f.pimax2 && b3 < kRppiTabReject;
+  bool ok = (pf + f.epi < f.pimax2) & (b3 < kRppiTabReject);
   // Order of the three rp^2: rho is monotone in rp^2, so rho_j < rho_l
   // proves A < B; equal rho leaves the order open.
-  ok = ok && rj != rl;
+  ok &= rj != rl;
   const bool jfirst = rj < rl;
   const float a = rj * rj, b = rl * rl;
   const float mn = jfirst ? a : b, mx = jfirst ? b : a;
-  const bool below = hi < mn, above = lo > mx, between = lo > mn && hi < mx;
-  ok = ok && (below || above || between);
+  const bool below = hi < mn, above = lo > mx, between = (lo > mn) & (hi < mx);
+  ok &= below | above | between;
   const int pos = below ? 0 : (above ? 2 : 1);  // anchor sides below rp3
-  // Triangle test.
-  const float p = -2.0f * fmaf(xj, xl, yj * yl);
-  ok = ok && fabsf(p) < fmaf(2.0f * rj, rl, f.hm);
+  // Triangle test: |p| < 2 rho_j rho_l - M with p = -2 (d_j.d_l)_xy, as
+  // |(d_j.d_l)_xy| < fma(rho_j, rho_l, -M/2) (both sides halved exactly).
+  ok &= fabsf(fmaf(xj, xl, yj * yl)) < fmaf(rj, rl, 0.5f * f.hm);
   // pi bin of the third side, needed when it is one of the two shortest.
   const int k = static_cast<int>(fminf(rppi_sqrt_est(pf), 4095.0f));
   const float k2 = static_cast<float>(k * k), k3 = static_cast<float>((k + 1) * (k + 1));
   const float w = f.epi + f.pmarg;
-  ok = ok && (pos == 2 || ((k == 0 || pf - w > k2) && pf + w < k3));
+  ok &= (pos == 2) | (((k == 0) | (pf - w > k2)) & (pf + w < k3));
   const unsigned ms = jfirst ? mj : ml, mL = jfirst ? ml : mj;
   const int rs = static_cast<int>(ms & 0xffffu), ps = static_cast<int>(ms >> 16);
   const int rL = static_cast<int>(mL & 0xffffu), pL = static_cast<int>(mL >> 16);
