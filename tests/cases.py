@@ -230,6 +230,18 @@ def rppi_small_box_nondivisible(seed=23):
     return C.uniform_box(1200, 100.0, seed), 100.0, C.linear_edges(30.0, 6), 12
 
 
+def rppi_small_box_tiny_grid(seed=28):
+    """L = 50, rpMax = 25 (two cells in x and y, so every x-y cell is visited
+    as two images), 15 pi bins (4 cells, the last 5 wide)."""
+    return C.uniform_box(300, 50.0, seed), 50.0, C.linear_edges(25.0, 5), 15
+
+
+def rppi_small_box_one_cell(seed=29):
+    """L = 20 below rpMax = 25 and piMax = 22: one cell per axis, so the 27
+    slots are 27 images of every point."""
+    return C.uniform_box(40, 20.0, seed), 20.0, C.linear_edges(25.0, 5), 22
+
+
 def rppi_small_survey(seed=24, nd=1500, nr=3000, weighted=False):
     """Survey wedge scaled down, jointly shifted; rp 8 log bins in [2, 30),
     20 pi bins (cells of sqrtf(30^2 + 20^2))."""

@@ -42,7 +42,8 @@ def test_rppi_known_answers(engine_lib, make):
 
 
 @pytest.mark.parametrize("make", [cases.rppi_small_box, cases.rppi_small_box_clustered,
-                                  cases.rppi_small_box_nondivisible], ids=lambda f: f.__name__)
+                                  cases.rppi_small_box_nondivisible, cases.rppi_small_box_tiny_grid,
+                                  cases.rppi_small_box_one_cell], ids=lambda f: f.__name__)
 def test_rppi_box_parity(engine_lib, oracle, make):
     p, box, edges, npi = make()
     h, st, out, bins, pis = run_rppi(box, edges, npi, p)
@@ -62,6 +63,16 @@ def test_rppi_box_distinct_catalogues(engine_lib, oracle):
         h, _, _, _, _ = run_rppi(box, edges, npi, *args)
         ref, _ = oracle.count_rppi(box, edges, npi, *args)
         assert np.array_equal(h, ref)
+
+
+def test_rppi_empty_partner_catalogues(engine_lib, oracle):
+    """Anchors with empty p2 and p3: every list is empty and nothing counts."""
+    p, box, edges, npi = cases.rppi_small_box(n=500)
+    empty = np.zeros((0, 4))
+    h, st, _, _, _ = run_rppi(box, edges, npi, p, empty, empty)
+    ref, _ = oracle.count_rppi(box, edges, npi, p, empty, empty)
+    assert not ref.any() and np.array_equal(h, ref)
+    assert st["overflow"] == 0 and st["n_pairs"] == 0
 
 
 @pytest.mark.parametrize("combo", ["DDD", "DDR", "DRR", "RRR"])
@@ -143,7 +154,8 @@ def test_rppi_reference_known_answers(ref, make):
 
 
 @pytest.mark.parametrize("make", [cases.rppi_small_box, cases.rppi_small_box_clustered,
-                                  cases.rppi_small_box_nondivisible], ids=lambda f: f.__name__)
+                                  cases.rppi_small_box_nondivisible, cases.rppi_small_box_tiny_grid,
+                                  cases.rppi_small_box_one_cell], ids=lambda f: f.__name__)
 def test_rppi_reference_box(ref, make):
     p, box, edges, npi = make()
     h_ref, ov_ref, _, _ = ref.reference_count_rppi(box, edges, npi, p)
