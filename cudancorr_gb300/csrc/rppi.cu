@@ -632,6 +632,9 @@ __global__ void k_rp_fold(unsigned long long* __restrict__ hu, double* __restric
 // with one copy, 20.6 with two, 20.0 with four, no gain beyond).
 constexpr long kRppiHistBudget = 64L << 20;
 constexpr int kRppiHistCopiesMax = 4;
+// Device memory for the per-warp neighbour lists; dense catalogues (long
+// lists) get fewer CTAs rather than a failed allocation.
+constexpr size_t kRppiSlabBudget = size_t{16} << 30;
 static int rppi_hist_copies(size_t bytes) {
   return static_cast<int>(std::max<long>(1, std::min<long>(kRppiHistCopiesMax, kRppiHistBudget / static_cast<long>(bytes))));
 }
@@ -894,13 +897,21 @@ int rppi_run(ncorr_handle* h, const double4_16a* d1, int n1, const double4_16a* 
                 "survey anchor on the upper face of the cell grid (unclamped cell index == nc)");
 
   const int cap = std::max(1, std::max(bound[0], bound[1]));
+  if (cap > kListMax)
+    return fail(NCORR_ERR_CAPACITY, "rppi: a 27-cell neighbourhood holds more than 2^24 points");
   const int occ = rppi_occupancy(g.survey != 0, sym, weighted);
   if (occ <= 0) return fail(NCORR_ERR_CUDA, "rppi kernel does not fit on the device");
   int nsm = 0;
   CU(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->device));
-  // Warps take kRppiChunk anchors at a time: no more CTAs than that needs.
+  // Warps take kRppiChunk anchors at a time: no more CTAs than that needs,
+  // and no more than keep the per-warp lists within kRppiSlabBudget.
   const long per_cta = static_cast<long>(kRppiWarps) * kRppiChunk;
-  const int grid = static_cast<int>(std::max(1L, std::min((n1 + per_cta - 1) / per_cta, static_cast<long>(nsm) * occ)));
+  const size_t entry_bytes =
+      sizeof(double4_16a) + sizeof(double2) + sizeof(float4) + sizeof(unsigned) + (weighted ? sizeof(double) : 0);
+  const size_t cta_bytes = static_cast<size_t>(kRppiWarps) * (sym ? 1 : 2) * cap * entry_bytes;
+  const long fit = std::max<long>(1, static_cast<long>(kRppiSlabBudget / cta_bytes));
+  const int grid = static_cast<int>(
+      std::max(1L, std::min({(n1 + per_cta - 1) / per_cta, static_cast<long>(nsm) * occ, fit})));
   const size_t slab_n = static_cast<size_t>(grid) * kRppiWarps * (sym ? 1 : 2) * cap;
   CU(h->rp_pos.ensure(slab_n * sizeof(double4_16a)));
   CU(h->rp_ab.ensure(slab_n * sizeof(double2)));
