@@ -46,12 +46,13 @@ N_SM = 152
 FP32_LANES_PER_SM = 128
 L2_FLUSH_BYTES = 256 << 20
 # Triangle-kernel DRAM traffic per launch (dram__bytes_read.sum +
-# dram__bytes_write.sum): 121.0 MB read + 2030.5 MB written, measured with ncu
-# on the 249,814-point box_clustered_L1000 workload (the writes are the
-# per-warp neighbour lists, written once per anchor, evicted from L2), scaled
-# by the anchor count to the 2,001,574-point box_clustered launch.
-TRIANGLE_KERNEL_DRAM_BYTES = {"box_clustered": int(2151.6e6 * 2001574 / 249814),
-                              "box_clustered_L1000": int(2151.6e6)}
+# dram__bytes_write.sum): 150.1 MB read + 1.5 MB written, measured with ncu
+# on the 249,814-point box_clustered_L1000 workload, scaled by the anchor
+# count to the 2,001,574-point box_clustered launch. The per-warp neighbour
+# lists (about 33 KB per anchor) stay out of DRAM: each warp discards their
+# L2 lines when its anchor is done.
+TRIANGLE_KERNEL_DRAM_BYTES = {"box_clustered": int(151.65e6 * 2001574 / 249814),
+                              "box_clustered_L1000": int(151.65e6)}
 
 
 def workload(name: str, seed_offset: int):

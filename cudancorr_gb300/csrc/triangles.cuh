@@ -542,6 +542,18 @@ __device__ __noinline__ void cold_flush_exact(Cold& c) {
 // Histogram update of the careful path. The key is the table-scaled code: a
 // byte offset into the shared histogram, or a plain bin index for the global
 // histogram (HG).
+// Drops the L2 lines of [p, p + bytes) without writing them back (the warp's
+// lanes take a line each). A warp's lists are dead once its anchor is done
+// and are rewritten before they are read again; left in L2, the next
+// anchors' traffic evicts them and they are written back to DRAM for
+// nothing. Skipped unless p is 128-byte aligned (the line size).
+__device__ __forceinline__ void discard_l2(const void* p, size_t bytes, int lane) {
+  const char* c = static_cast<const char*>(p);
+  if (reinterpret_cast<uintptr_t>(c) & 127u) return;
+  for (size_t off = static_cast<size_t>(lane) * 128; off < bytes; off += 32 * 128)
+    asm volatile("discard.global.L2 [%0], 128;" ::"l"(c + off) : "memory");
+}
+
 template <bool WEIGHTED, bool HG>
 __device__ __forceinline__ void hist_add(unsigned char* hist_s, const HistOut& hist, unsigned key, float w) {
   if (HG) {
@@ -1353,6 +1365,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_triangles(KArgs a) {
       }
       if (qn > 0) cold_drain<SURVEY, WEIGHTED, HG>(c, lb, k3, qn);
     }
+    __syncwarp();  // every lane has read the lists for the last time
+    discard_l2(l2.v, static_cast<size_t>(k2 + kListPad) * sizeof(ListEnt), lane);
+    if (WEIGHTED) discard_l2(l2.w, static_cast<size_t>(k2 + kListPad) * sizeof(float), lane);
+    if (!SYM) {
+      discard_l2(l3.v, static_cast<size_t>(k3) * sizeof(ListEnt), lane);
+      if (WEIGHTED) discard_l2(l3.w, static_cast<size_t>(k3) * sizeof(float), lane);
+    }
+    __syncwarp();  // the discards precede the next anchor's list writes
   }
   if (lane == 0 && held) atomicAdd(&s_slot, ~0ull);
   cold_flush_exact<SURVEY, WEIGHTED>(c);
