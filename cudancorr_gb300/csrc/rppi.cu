@@ -732,32 +732,14 @@ int rppi_init(ncorr_handle* h, const double box[3], const double* edges, int n_e
   g.f_rp_lo = rpmin > 2.0 * slack ? f32_down((rpmin - 2.0 * slack) * (rpmin - 2.0 * slack)) : 0.0f;
   const double smax = std::sqrt(g.sqr_rmax);
   g.f_s_hi = f32_up((smax + 2.0 * slack) * (smax + 2.0 * slack));
-  // Gather prefilter. A valid point has |coordinate| < X = (nc + 1) cell per
-  // axis, and box <= nc cell. The FP32 offset of a neighbour in a box is
-  // fl(fl(fl(q) + fl(shift)) - fl(p1)), within u (5 X + |D|) of the true
-  // offset D (u = 2^-24, |D| < 2 cells); in a survey fl(fl(q) - fl(p1)),
-  // within u (2 X + |D|). The reference's own FP64 offset lies within
-  // 2^-50 X of D. With E the per-axis bound, the FP32 rp (pi, s) estimate is
-  // within |E_xy| (E_z, |E|) of the reference's, and the FP32 squares err by
-  // at most (1 + u)^2 (1 + u, (1 + u)^3) relatively; each threshold below adds
-  // those, plus a relative 2^-40 that covers the reference's FP64 rounding of
-  // the squares, so an estimate past it proves the reference cuts the point.
+  // Gather prefilter (thresholds derived at rppi_gather_cut).
   {
-    const double u = std::ldexp(1.0, -24);
-    double e[3];
-    for (int d = 0; d < 3; ++d) {
-      const double X = (g.nc[d] + 1.0) * g.cell[d];
-      e[d] = u * ((is_survey ? 2.0 : 5.0) * X + 2.0 * g.cell[d]) * (1.0 + 1e-6) + std::ldexp(X, -50);
-      g.fbox[d] = static_cast<float>(box[d]);
-    }
-    const double r40 = std::ldexp(1.0, -40);
-    const double er = std::sqrt(e[0] * e[0] + e[1] * e[1]) + rpmax * r40;
-    const double ez = e[2] + pimax * r40;
-    const double es = std::sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]) + smax * r40;
-    g.a_rp_hi = f32_up((rpmax + er) * (rpmax + er) * (1.0 + u) * (1.0 + u) * (1.0 + r40));
-    g.a_rp_lo = rpmin > er ? f32_down((rpmin - er) * (rpmin - er) * (1.0 - u) * (1.0 - u) * (1.0 - r40)) : -1.0f;
-    g.a_pi_hi = f32_up((pimax + ez) * (pimax + ez) * (1.0 + u) * (1.0 + r40));
-    g.a_s_hi = f32_up((smax + es) * (smax + es) * (1.0 + u) * (1.0 + u) * (1.0 + u) * (1.0 + r40));
+    const RppiGatherCut gc = rppi_gather_cut(g.nc, g.cell, is_survey != 0, rpmin, rpmax, pimax);
+    g.a_rp_hi = gc.rp_hi;
+    g.a_rp_lo = gc.rp_lo;
+    g.a_pi_hi = gc.pi_hi;
+    g.a_s_hi = gc.s_hi;
+    for (int d = 0; d < 3; ++d) g.fbox[d] = static_cast<float>(box[d]);
   }
   // The box-mode FP32 classifier: its bands and margins, derived in
   // rppi_fast.cuh (u = 2^-24).

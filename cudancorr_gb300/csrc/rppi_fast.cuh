@@ -81,6 +81,53 @@ inline void rppi_build_table(const RppiFast& f, const float* e2lo, const float* 
   }
 }
 
+// Thresholds of the neighbour gather's FP32 prefilter, which drops the
+// points that the reference certainly cuts against the anchor before the
+// FP64 test. A valid point has |coordinate| < X = (nc + 1) cell per axis
+// (the cell list clamps the upper face into the last cell), and box <= nc
+// cell, so an offset D = q + shift - p1 has |D| < 3X. The kernel's FP32
+// offset of a neighbour in a box is fl(fl(fl(q) + fl(shift)) - fl(p1)):
+// roundings of at most uX, uX, 2uX, uX and u|D| (u = 2^-24) put it within
+// 8uX of D; in a survey fl(fl(q) - fl(p1)) is within 4uX. The reference's
+// own FP64 offset lies within 2^-50 X of D. With E the per-axis bound, the FP32 rp (pi, s) estimate is
+// within |E_xy| (E_z, |E|) of the reference's, and the FP32 squares err by
+// at most (1 + u)^2 (1 + u, (1 + u)^3) relatively; each threshold adds
+// those, plus a relative 2^-40 that covers the reference's FP64 rounding of
+// the squares, so an estimate past it proves the reference cuts the point:
+// box rp^2 > rp_hi or < rp_lo (-1: no lower cut) or dz^2 > pi_hi, survey
+// s^2 > s_hi.
+struct RppiGatherCut {
+  float rp_hi, rp_lo, pi_hi, s_hi;
+};
+
+inline RppiGatherCut rppi_gather_cut(const int nc[3], const double cell[3], bool survey, double rpmin, double rpmax,
+                                     double pimax) {
+  auto up = [](double x) {
+    float f = static_cast<float>(x);
+    return static_cast<double>(f) < x ? std::nextafter(f, INFINITY) : f;
+  };
+  auto down = [](double x) {
+    float f = static_cast<float>(x);
+    return static_cast<double>(f) > x ? std::nextafter(f, -INFINITY) : f;
+  };
+  const double u = std::ldexp(1.0, -24), r40 = std::ldexp(1.0, -40);
+  double e[3];
+  for (int d = 0; d < 3; ++d) {
+    const double X = (nc[d] + 1.0) * cell[d];
+    e[d] = u * (survey ? 4.0 : 8.0) * X * (1.0 + 1e-6) + std::ldexp(X, -50);
+  }
+  const double smax = std::sqrt(rpmax * rpmax + pimax * pimax);
+  const double er = std::sqrt(e[0] * e[0] + e[1] * e[1]) + rpmax * r40;
+  const double ez = e[2] + pimax * r40;
+  const double es = std::sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]) + smax * r40;
+  RppiGatherCut c;
+  c.rp_hi = up((rpmax + er) * (rpmax + er) * (1.0 + u) * (1.0 + u) * (1.0 + r40));
+  c.rp_lo = rpmin > er ? down((rpmin - er) * (rpmin - er) * (1.0 - u) * (1.0 - u) * (1.0 - r40)) : -1.0f;
+  c.pi_hi = up((pimax + ez) * (pimax + ez) * (1.0 + u) * (1.0 + r40));
+  c.s_hi = up((smax + es) * (smax + es) * (1.0 + u) * (1.0 + u) * (1.0 + u) * (1.0 + r40));
+  return c;
+}
+
 // An estimate of sqrt(x) for x >= 0; its error only costs certainty (the
 // pi-bin test below checks the bin it gives against margins).
 __host__ __device__ inline float rppi_sqrt_est(float x) {

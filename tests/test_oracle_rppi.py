@@ -154,6 +154,28 @@ def test_rppi_golden_reference_outputs(oracle, meta_path):
         assert ov == meta["overflow"]
 
 
+def test_rppi_gather_prefilter_never_drops_a_kept_point(tmp_path):
+    """The FP32 prefilter of the rppi neighbour gather (rppi_gather_cut in
+    cudancorr_gb300/csrc/rppi_fast.cuh), with the kernel's FP32 operations
+    repeated on the host, against the reference's FP64 cut: neighbours on the
+    cut surfaces to a few 2^-20 relative, at coordinates up to the grid's far
+    face and through periodic images, in two boxes and a survey extent."""
+    import shutil
+    import subprocess
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    src = GOLDEN.parent / "cpp" / "rppi_gather_check.cu"
+    exe = tmp_path / "rppi_gather_check"
+    r = subprocess.run([nvcc, "-std=c++17", "-O2", "-Xcompiler", "-ffp-contract=off", "-o", str(exe), str(src)],
+                       capture_output=True, text=True)
+    if r.returncode != 0:
+        pytest.skip(f"nvcc could not build the host check: {r.stderr[:200]}")
+    for seed in (1, 2):
+        out = subprocess.run([str(exe), "100000", str(seed)], capture_output=True, text=True)
+        assert out.returncode == 0, out.stdout + out.stderr
+        n = dict(zip(out.stdout.split()[0::2], map(int, out.stdout.split()[1::2])))
+        assert n["violations"] == 0 and n["near"] > n["checked"] // 100 and n["kept"] > n["checked"] // 10
+
+
 def test_rppi_fp32_classifier_agrees_with_the_exact_computation(tmp_path):
     """The box-mode FP32 classifier (cudancorr_gb300/csrc/rppi_fast.cuh),
     compiled for the host, against an FP64 restatement of the reference on
