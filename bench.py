@@ -895,6 +895,102 @@ def run_reference_rppi(args) -> dict:
     }
 
 
+def run_rppi_survey(args) -> dict:
+    """The rppi bin type in survey mode on one GPU: DDD of the survey wedge's
+    data (unit weights, so that triangles are counted) on a seeded 1/8 anchor
+    sample, all data as p2 and p3; rp in 12 log bins on [1, 30), 30 unit pi
+    bins. Every pair an FP32 estimate does not certainly cut is evaluated in
+    FP64 (line-of-sight projections), 32 lanes wide."""
+    import torch
+    from cudancorr_gb300 import api
+
+    world, rank, local = dist_setup()
+    d, _, box, ori, _ = survey_catalogues(7 + 10 * rank)
+    d = np.ascontiguousarray(d)
+    d[:, 3] = 1.0
+    edges = api.logspace(1.0, 30.0, 13)
+    rng = np.random.default_rng(3)
+    sub = np.ascontiguousarray(d[np.sort(rng.choice(len(d), len(d) // 8, replace=False))])
+    dev = torch.device("cuda", local)
+    t_d, t_s = torch.from_numpy(d).to(dev), torch.from_numpy(sub).to(dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    corr = api.ncorr(box, api.rppi, edges, RPPI_NPI, True, ori)
+
+    def device_step():
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        corr._calculate_device(t_s, t_d, t_d, stream=stream.cuda_stream)
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1), corr.stats()
+
+    for _ in range(args.warmup):
+        device_step()
+    sampler = ClockSampler(local)
+    sampler.start()
+    barrier(world)
+    step_ms, kernel_ms, tri = [], [], []
+    for _ in range(args.steps):
+        ms, st = device_step()
+        step_ms.append(ms)
+        kernel_ms.append(st["ms_count"])
+        tri.append(st["triangles"])
+    barrier(world)
+    clocks = sampler.stop()
+    st_last = corr.stats()
+    total_ms = barrier_max(sum(step_ms), world)
+    total_tri = barrier_sum(float(sum(tri)), world)
+    s_host = torch.from_numpy(sub).pin_memory().numpy()
+    d_host = torch.from_numpy(d).pin_memory().numpy()
+    corr.calculateD1D2D3(s_host, d_host, d_host)
+    barrier(world)
+    e2e_ms = []
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        corr.calculateD1D2D3(s_host, d_host, d_host)
+        _ = corr.getTriCountsOut()
+        e2e_ms.append((time.perf_counter() - t) * 1e3)
+    e2e_total = barrier_max(sum(e2e_ms), world)
+    n_out = len(corr.getTriCountsOut())
+    corr.close()
+    nb = len(edges) - 1
+    sm_mhz = clocks.get("sm_mhz") or 1995.0
+    peak_tflops = N_SM * FP32_LANES_PER_SM * 2 * sm_mhz * 1e6 / 1e12
+    achieved = 8.0 * st_last["n_pairs"] / (statistics.mean(kernel_ms) / 1e3) / 1e12
+    return {
+        "metric": METRIC, "value": total_tri / (total_ms / 1e3), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp64 exact (fp32 prefilter)",
+        "data": "synthetic (seeded)",
+        "config": {"workload": "rppi_survey",
+                   "description": "survey wedge data (500,000 points, unit weights), DDD on a 1/8 anchor sample; "
+                                  "rppi: rp 12 log bins in [1,30), 30 unit pi bins",
+                   "n_points": int(len(d)), "anchors": int(len(sub)), "rp_bins": nb, "pi_bins": RPPI_NPI,
+                   "triangles_per_step": int(tri[-1]), "overflow_per_step": float(st_last["overflow"]),
+                   "l2": "flushed (256 MiB write) between steps",
+                   "parallelism": f"{world} independent catalogue(s), one per GPU"},
+        "e2e": {"value": total_tri / (e2e_total / 1e3), "unit": UNIT,
+                "h2d_bytes_per_step": int(sub.nbytes + d.nbytes), "d2h_bytes_per_step": int(nb ** 3 * RPPI_NPI ** 2 * 8),
+                "ms_per_step": e2e_total / args.steps},
+        "roofline": {"bound": "fp32_issue", "achieved": achieved, "peak": peak_tflops, "unit": "TFLOP/s",
+                     "frac": achieved / peak_tflops, "traffic": None, "kernel": "k_rppi",
+                     "kernel_ms": statistics.mean(kernel_ms),
+                     "work": "8 flops x candidate pairs visited per launch, as for the box",
+                     "note": "survey pairs are evaluated in FP64, whose pipe runs at 1/64 of the FP32 rate",
+                     "pairs_visited": int(st_last["n_pairs"]), "pairs_fp64": int(st_last["n_exact_tris"]),
+                     "peak_basis": "152 SMs x 128 FP32 lanes x 2 x median sampled SM clock"},
+        "gpu_launches": engine_launches(2, True, rppi=True) * args.steps,
+        "clocks": clocks,
+        "n_out": n_out,
+    }
+
+
 def run_reference(args) -> dict:
     """The reference's own kernel (oracle/_ref cubin, compiled unmodified from
     its source/device.cu) behind a restatement of its host flow, on an anchor
@@ -922,7 +1018,7 @@ def run_reference(args) -> dict:
         return {"impl": "reference", "unavailable": f"reference kernel not loadable: {e}"}
     if args.workload == "rppi_box_clustered":
         return run_reference_rppi(args)
-    if args.workload in ("batch_mocks", "survey"):
+    if args.workload in ("batch_mocks", "survey", "rppi_survey"):
         return {"impl": "reference", "unavailable": "the reference arm times the single-catalogue box workloads; "
                                                     f"{args.workload} would take the reference kernel hours"}
     p, box, edges, desc = workload(args.workload, 0)
@@ -973,7 +1069,7 @@ def main():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--workload", default="box_clustered",
                     choices=["box_clustered", "box_clustered_L1000", "box_uniform", "soneira_peebles",
-                             "batch_mocks", "survey", "rppi_box_clustered"])
+                             "batch_mocks", "survey", "rppi_box_clustered", "rppi_survey"])
     ap.add_argument("--schedule", default="dynamic", choices=["dynamic", "static", "learned"],
                     help="anchor order of the triangle kernel (learned: trains the work model first)")
     ap.add_argument("--no-autotune", action="store_true", help="batch_mocks: default tuning")
@@ -998,6 +1094,8 @@ def main():
         out = run_survey(args)
     elif args.workload == "rppi_box_clustered":
         out = run_rppi(args)
+    elif args.workload == "rppi_survey":
+        out = run_rppi_survey(args)
     else:
         out = run_engine(args)
     if out is not None:

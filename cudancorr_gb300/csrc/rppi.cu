@@ -306,6 +306,14 @@ __device__ __forceinline__ int rppi_settle(const RppiArgs& a, const double4_16a&
   if (SURVEY) {
     x = sqr_sum_exact(dx, dy, dz, g.fma_pattern);  // sqrSep(p1, q), >= +0
     keep = act && dlt_pos(x, g.sqr_rmax) && dlt_pos(g.sqr_rmin, x);
+    // A side outside the rp and pi ranges for every partner's line of sight
+    // takes part in no counted triangle: it is not kept.
+    const float ax = __double2float_rn(__dsub_rn(p1.x, g.ori_x)), ay = __double2float_rn(p1.y),
+                az = __double2float_rn(p1.z);
+    const float4 los = make_float4(ax, ay, az, sqrtf(fmaf(az, az, fmaf(ay, ay, ax * ax))));
+    keep = keep && !rppi_los_cut(__double2float_rn(dx), __double2float_rn(dy), __double2float_rn(dz),
+                                 __double2float_rn(x), los, g.los_smax, g.fast.pimax2, g.fast.rpmax2_hi,
+                                 g.fast.rpmin2_lo);
   } else {
     y = __dmul_rn(dz, dz);
     x = rp_exact(dx, dy, g.rp_pattern);  // >= +0
@@ -740,6 +748,7 @@ int rppi_init(ncorr_handle* h, const double box[3], const double* edges, int n_e
     g.a_pi_hi = gc.pi_hi;
     g.a_s_hi = gc.s_hi;
     for (int d = 0; d < 3; ++d) g.fbox[d] = static_cast<float>(box[d]);
+    g.los_smax = f32_up(std::sqrt(g.sqr_rmax));
   }
   // The box-mode FP32 classifier: its bands and margins, derived in
   // rppi_fast.cuh (u = 2^-24).

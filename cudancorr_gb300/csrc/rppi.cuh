@@ -39,6 +39,7 @@ struct RppiGeom {
   float a_rp_hi;     // box: rp^2 estimate > a_rp_hi  => rp^2 >= rpMax^2
   float a_rp_lo;     // box: rp^2 estimate < a_rp_lo  => rp^2 <= rpMin^2 (-1: never)
   float a_s_hi;      // survey: s^2 estimate > a_s_hi => s^2 >= sqrRMax
+  float los_smax;    // survey: smallest float >= sqrt(sqrRMax), for rppi_los_cut
   long long nbins;   // nb^3 * nPi^2
   // Box mode: the FP32 classifier (rppi_fast.cuh) and its bin-edge bounds.
   RppiFast fast;

@@ -128,6 +128,39 @@ inline RppiGatherCut rppi_gather_cut(const int nc[3], const double cell[3], bool
   return c;
 }
 
+// Survey mode: whether the anchor side (p1, q), with FP32 offset d = p1 - q
+// and s^2 = s2, is certainly cut for every partner of the list. The
+// reference's line of sight for a pair is L = 3A + (pj - p1) + (pl - p1),
+// A = (p1.x - ori.x, p1.y, p1.z) (source/device.cu:45-56); both partners
+// lie within sMax of p1, so L is within the angle phi of A, sin(phi) <=
+// (s + sMax) / (3 |A|). With theta_A the angle between d and A, the side's
+// |cos(theta)| against L lies between cos(theta_A + phi) (0 past pi/2) and
+// cos(theta_A - phi) (1 below 0), so pi^2 = s^2 cos^2 and rp^2 = s^2 sin^2
+// are bounded for every partner; the side is cut when pi^2 >= piMax^2, rp^2
+// >= rpMax^2 or rp^2 <= rpMin^2 over the whole range (the reference keeps
+// rpMin^2 < rp^2 < rpMax^2 and pi^2 < piMax^2 for both anchor sides,
+// source/device.cu:483-490). The FP32 evaluation errs by a few 2^-24
+// relatively; the margins (1e-5 on cos, 1e-4 on sin(phi), 1e-5 on the
+// squares) exceed that and the reference's FP64 rounding by far.
+// los = (A in FP32, |A|); smax >= sMax; pimax2, rpmax2 >= and rpmin2 <= the
+// squared limits.
+__host__ __device__ inline bool rppi_los_cut(float dx, float dy, float dz, float s2, float4 los, float smax,
+                                             float pimax2, float rpmax2, float rpmin2) {
+  const float s = sqrtf(s2);
+  const float sp = (s + smax) / (3.0f * los.w) * 1.0001f + 1e-6f;
+  if (!(sp < 0.999f) || !(s2 > 0.0f)) return false;
+  const float cp = sqrtf(1.0f - sp * sp);
+  const float c = fabsf(dx * los.x + dy * los.y + dz * los.z) / (s * los.w);
+  const float cl = fmaxf(c - 1e-5f, 0.0f), ch = fminf(c + 1e-5f, 1.0f);
+  const float sah = sqrtf(fmaxf(1.0f - cl * cl, 0.0f));
+  const float cmin = fmaxf(cl * cp - sah * sp - 1e-6f, 0.0f);
+  const float cmax = ch >= cp ? 1.0f : fminf(ch + sah * sp + 1e-6f, 1.0f);
+  const float lo = s2 * (1.0f - 1e-5f), hi = s2 * (1.0f + 1e-5f);
+  return (lo * cmin * cmin >= pimax2 * (1.0f + 1e-5f)) |
+         (lo * (1.0f - cmax * cmax) - 1e-5f * hi >= rpmax2 * (1.0f + 1e-5f)) |
+         (hi * (1.0f - cmin * cmin) + 1e-5f * hi <= rpmin2 * (1.0f - 1e-5f));
+}
+
 // An estimate of sqrt(x) for x >= 0; its error only costs certainty (the
 // pi-bin test below checks the bin it gives against margins).
 __host__ __device__ inline float rppi_sqrt_est(float x) {

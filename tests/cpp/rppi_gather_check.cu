@@ -7,9 +7,13 @@
 // surfaces (rp = rpMax, rp = rpMin, |dz| = piMax, s = sMax, to within a few
 // 2^-20 relative), at coordinates up to the grid's far face and through the
 // periodic images.
+// Survey mode also drops list entries that are outside the rp and pi ranges
+// for every partner's line of sight (rppi_los_cut); each entry it drops is
+// tested against the reference's anchor-side test with partners that tilt
+// the line of sight as far as the list allows.
 //   rppi_gather_check <n_per_kind> <seed>
-// prints "checked <n> kept <k> dropped <d> near <m> violations <v>" and exits
-// 1 on a violation (a kept point dropped).
+// prints "checked <n> kept <k> dropped <d> near <m> violations <v> los_cut
+// <c> los_partners <p> los_violations <w>" and exits 1 on a violation.
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -149,6 +153,115 @@ int main(int argc, char** argv) {
       }
     }
   }
-  std::printf("checked %ld kept %ld dropped %ld near %ld violations %ld\n", checked, kept, dropped, near, violations);
-  return violations ? 1 : 0;
+  // The survey line-of-sight cut. The reference's dotProduct_d3 and sqrSep as
+  // nvcc contracts them: fma(a.z, b.z, fma(a.x, b.x, a.y * b.y)).
+  long los_checked = 0, los_cut = 0, los_partners = 0, los_violations = 0;
+  {
+    const double rpmin = 2.0, rpmax = 30.0, pimax = 20.0;
+    const double sqr_rpmin = rpmin * rpmin, sqr_rpmax = rpmax * rpmax, sqr_pimax = pimax * pimax;
+    const double sqr_rmax = sqr_rpmax + sqr_pimax, smax = std::sqrt(sqr_rmax);
+    auto up = [](double x) {
+      float f = static_cast<float>(x);
+      return static_cast<double>(f) < x ? std::nextafter(f, INFINITY) : f;
+    };
+    auto down = [](double x) {
+      float f = static_cast<float>(x);
+      return static_cast<double>(f) > x ? std::nextafter(f, -INFINITY) : f;
+    };
+    const float smax_f = up(smax), pimax2_f = static_cast<float>(sqr_pimax), rpmax2_f = up(sqr_rpmax),
+                rpmin2_f = down(sqr_rpmin);
+    auto dot = [](const double a[3], const double b[3]) { return std::fma(a[2], b[2], std::fma(a[0], b[0], a[1] * b[1])); };
+    auto unit = [&](double v[3]) {
+      const double n = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+      for (int d = 0; d < 3; ++d) v[d] /= n;
+    };
+    std::normal_distribution<double> N(0.0, 1.0);
+    for (long it = 0; it < n_per_kind; ++it) {
+      // Anchor, observer offset (only ori.x enters the reference's line of
+      // sight) and A; |A| from 60 (wide tilt) to 3000.
+      const double ori_x = (U(rng) - 0.5) * 200.0;
+      double dir[3] = {N(rng), N(rng), N(rng)};
+      unit(dir);
+      const double an = 60.0 * std::pow(50.0, U(rng));
+      const double p1[3] = {ori_x + an * dir[0], an * dir[1], an * dir[2]};
+      const double A[3] = {p1[0] - ori_x, p1[1], p1[2]};
+      // Entry on the cylinder's surfaces as seen along A, or anywhere in the
+      // sphere: offset d = p1 - pj at |d| < sMax.
+      double e1[3] = {N(rng), N(rng), N(rng)};
+      const double ad = dot(e1, dir);
+      for (int d = 0; d < 3; ++d) e1[d] -= ad * dir[d];
+      unit(e1);
+      const int kind = static_cast<int>(U(rng) * 4.0);
+      const double wig = 1.0 + (U(rng) - 0.5) * 0.2;
+      double along = (2.0 * U(rng) - 1.0) * pimax, across = rpmax * std::sqrt(U(rng));
+      if (kind == 0) along = (U(rng) < 0.5 ? -1.0 : 1.0) * pimax * wig;
+      if (kind == 1) across = rpmax * wig;
+      if (kind == 2) across = rpmin * wig;
+      double dv[3];
+      for (int d = 0; d < 3; ++d) dv[d] = along * dir[d] + across * e1[d];
+      if (kind == 3)
+        for (int d = 0; d < 3; ++d) dv[d] = (2.0 * U(rng) - 1.0) * smax;
+      const double pj[3] = {p1[0] - dv[0], p1[1] - dv[1], p1[2] - dv[2]};
+      double d64[3] = {p1[0] - pj[0], p1[1] - pj[1], p1[2] - pj[2]};
+      const double s2 = dot(d64, d64);
+      if (!(s2 < sqr_rmax && s2 > 0.0)) continue;
+      ++los_checked;
+      // The kernel's inputs: FP32 offset, s^2 and A.
+      const float ax = static_cast<float>(A[0]), ay = static_cast<float>(A[1]), az = static_cast<float>(A[2]);
+      const float4 los = {ax, ay, az, std::sqrt(std::fma(az, az, std::fma(ay, ay, ax * ax)))};
+      if (!ncorr_gb300::rppi_los_cut(static_cast<float>(d64[0]), static_cast<float>(d64[1]),
+                                     static_cast<float>(d64[2]), static_cast<float>(s2), los, smax_f, pimax2_f,
+                                     rpmax2_f, rpmin2_f))
+        continue;
+      ++los_cut;
+      // Partners within sMax: the directions that tilt L towards and away
+      // from d and across, at the sphere's edge, and random ones.
+      double perp[3] = {dv[1] * dir[2] - dv[2] * dir[1], dv[2] * dir[0] - dv[0] * dir[2],
+                        dv[0] * dir[1] - dv[1] * dir[0]};
+      double dperp[3];
+      const double dd = dot(dv, dir);
+      for (int d = 0; d < 3; ++d) dperp[d] = dv[d] - dd * dir[d];
+      const bool has_perp = dot(perp, perp) > 1e-20 && dot(dperp, dperp) > 1e-20;
+      if (has_perp) {
+        unit(perp);
+        unit(dperp);
+      }
+      for (int k = 0; k < 24; ++k) {
+        double w[3];
+        if (k < 6 && has_perp) {
+          const double* b = k < 2 ? dperp : (k < 4 ? perp : dir);
+          for (int d = 0; d < 3; ++d) w[d] = (k % 2 ? -1.0 : 1.0) * b[d];
+        } else {
+          w[0] = N(rng), w[1] = N(rng), w[2] = N(rng);
+          unit(w);
+        }
+        const double r = smax * (k < 12 ? 0.999999 : U(rng));
+        const double pl[3] = {p1[0] + r * w[0], p1[1] + r * w[1], p1[2] + r * w[2]};
+        double dl[3] = {p1[0] - pl[0], p1[1] - pl[1], p1[2] - pl[2]};
+        const double s2l = dot(dl, dl);
+        if (!(s2l < sqr_rmax && s2l > 0.0)) continue;
+        ++los_partners;
+        // getLOS, getSqrSdotL, getSqrRpSqrPi (source/device.cu:45-68) for
+        // the side (p1, pj).
+        const double L[3] = {((p1[0] - ori_x) + (pj[0] - ori_x)) + (pl[0] - ori_x), (p1[1] + pj[1]) + pl[1],
+                             (p1[2] + pj[2]) + pl[2]};
+        const double sqrL = dot(L, L);
+        const double t = dot(L, d64);
+        const double q1 = t * t;
+        const bool cut_here = sqr_pimax * sqrL < q1;
+        const double pi1 = q1 / sqrL, rp1 = s2 - pi1;
+        const bool side_ok = !cut_here && rp1 < sqr_rpmax && rp1 > sqr_rpmin && pi1 < sqr_pimax;
+        if (side_ok) {
+          if (los_violations < 10)
+            std::printf("los violation: A %.6g d (%.9g %.9g %.9g) pl (%.9g %.9g %.9g) rp1 %.9g pi1 %.9g\n", an,
+                        d64[0], d64[1], d64[2], dl[0], dl[1], dl[2], rp1, pi1);
+          ++los_violations;
+        }
+      }
+    }
+  }
+  std::printf("checked %ld kept %ld dropped %ld near %ld violations %ld los_checked %ld los_cut %ld los_partners %ld "
+              "los_violations %ld\n",
+              checked, kept, dropped, near, violations, los_checked, los_cut, los_partners, los_violations);
+  return violations || los_violations ? 1 : 0;
 }

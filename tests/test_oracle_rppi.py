@@ -159,7 +159,9 @@ def test_rppi_gather_prefilter_never_drops_a_kept_point(tmp_path):
     cudancorr_gb300/csrc/rppi_fast.cuh), with the kernel's FP32 operations
     repeated on the host, against the reference's FP64 cut: neighbours on the
     cut surfaces to a few 2^-20 relative, at coordinates up to the grid's far
-    face and through periodic images, in two boxes and a survey extent."""
+    face and through periodic images, in two boxes and a survey extent. Also
+    the survey line-of-sight cut of list entries (rppi_los_cut): no entry it
+    drops passes the reference's anchor-side test with any of its partners."""
     import shutil
     import subprocess
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
@@ -174,6 +176,7 @@ def test_rppi_gather_prefilter_never_drops_a_kept_point(tmp_path):
         assert out.returncode == 0, out.stdout + out.stderr
         n = dict(zip(out.stdout.split()[0::2], map(int, out.stdout.split()[1::2])))
         assert n["violations"] == 0 and n["near"] > n["checked"] // 100 and n["kept"] > n["checked"] // 10
+        assert n["los_violations"] == 0 and n["los_cut"] > n["los_checked"] // 10 and n["los_partners"] > 0
 
 
 def test_rppi_fp32_classifier_agrees_with_the_exact_computation(tmp_path):
