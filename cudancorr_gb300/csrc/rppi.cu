@@ -54,20 +54,56 @@ __device__ __forceinline__ double dot3_exact(double ax, double ay, double az, do
   }
 }
 
+// a < b for doubles a, b >= +0: the IEEE order of non-negative values is
+// the integer order of their bits. Integer compares keep the FP64 pipe,
+// a small fraction of the FP32 rate on this GPU, for arithmetic.
+__device__ __forceinline__ bool dlt_pos(double a, double b) {
+  return __double_as_longlong(a) < __double_as_longlong(b);
+}
+
+// exact_bin for r >= +0 with integer compares (sqr_bins are >= +0).
+__device__ __forceinline__ int exact_bin_pos(double r, const double* sb, int nb) {
+  const long long rb = __double_as_longlong(r);
+  int lo = 0, hi = nb - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (rb >= __double_as_longlong(sb[mid]))
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+// The same integer compare against a limit, for any non-NaN a: a < T when
+// T > +0, and a > T when T >= +0 (a negative a, or -0, has a negative
+// integer image, below every non-negative one).
+__device__ __forceinline__ bool dlt_lim(double a, double t) {
+  return __double_as_longlong(a) < __double_as_longlong(t);
+}
+__device__ __forceinline__ bool dgt_lim(double a, double t) {
+  return __double_as_longlong(a) > __double_as_longlong(t);
+}
+__device__ __forceinline__ bool deq_pos(double a, double b) {
+  return __double_as_longlong(a) == __double_as_longlong(b);
+}
+
 // getTriangleIndexRppi (source/device.cu:203-255). Returns -1 when the FP32
 // triangle test rejects; the index may reach nbins + nPi - 1 (pi bin nPi).
+// Every caller has checked r1, r2, r3 > rpMin^2 >= 0, so the sort and the bin
+// searches compare the values' bits.
 __device__ __forceinline__ long long rppi_index(double r1, double r2, double r3, double q1, double q2, double q3,
                                                 const double* sb, int nb, int npi) {
   double t;
-  if (r1 > r2) {
+  if (dlt_pos(r2, r1)) {
     t = r1; r1 = r2; r2 = t;
     t = q1; q1 = q2; q2 = t;
   }
-  if (r1 > r3) {
+  if (dlt_pos(r3, r1)) {
     t = r1; r1 = r3; r3 = t;
     t = q1; q1 = q3; q3 = t;
   }
-  if (r2 > r3) {
+  if (dlt_pos(r3, r2)) {
     t = r2; r2 = r3; r3 = t;
     t = q2; q2 = q3; q3 = t;
   }
@@ -75,9 +111,9 @@ __device__ __forceinline__ long long rppi_index(double r1, double r2, double r3,
   const float s2 = __fsqrt_rn(__double2float_rn(r2));
   const float s3 = __fsqrt_rn(__double2float_rn(r3));
   if (__fadd_rn(s1, s2) <= s3) return -1;
-  const long long i1 = exact_bin(r1, sb, nb);
-  const long long i2 = exact_bin(r2, sb, nb);
-  const long long i3 = exact_bin(r3, sb, nb);
+  const long long i1 = exact_bin_pos(r1, sb, nb);
+  const long long i2 = exact_bin_pos(r2, sb, nb);
+  const long long i3 = exact_bin_pos(r3, sb, nb);
   const long long p1 = static_cast<long long>(floorf(__fsqrt_rn(__double2float_rn(q1))));
   const long long p2 = static_cast<long long>(floorf(__fsqrt_rn(__double2float_rn(q2))));
   const long long P = npi, B = nb;
@@ -109,27 +145,6 @@ __device__ __forceinline__ void rppi_red_u64(bool p, unsigned long long* addr, u
       :
       : "r"(static_cast<unsigned>(p)), "l"(addr), "l"(v)
       : "memory");
-}
-
-// a < b for doubles a, b >= +0: the IEEE order of non-negative values is
-// the integer order of their bits. Integer compares keep the FP64 pipe,
-// a small fraction of the FP32 rate on this GPU, for arithmetic.
-__device__ __forceinline__ bool dlt_pos(double a, double b) {
-  return __double_as_longlong(a) < __double_as_longlong(b);
-}
-
-// exact_bin for r >= +0 with integer compares (sqr_bins are >= +0).
-__device__ __forceinline__ int exact_bin_pos(double r, const double* sb, int nb) {
-  const long long rb = __double_as_longlong(r);
-  int lo = 0, hi = nb - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (rb >= __double_as_longlong(sb[mid]))
-      lo = mid;
-    else
-      hi = mid - 1;
-  }
-  return lo;
 }
 
 // Per point: the reference's host cell (clamped, source/cudaNcorr.cu:50-58),
@@ -418,15 +433,15 @@ __device__ __forceinline__ void rppi_exact_pair(const RppiArgs& a, const RppiOut
   if (!SURVEY) {
     const double dz = __dsub_rn(pj.z, pl.z);
     const double pi3 = __dmul_rn(dz, dz);
-    if (!(pi3 < g.sqr_pimax)) return;
+    if (!dlt_pos(pi3, g.sqr_pimax)) return;
     const double rp3 = rp_exact(__dsub_rn(pj.x, pl.x), __dsub_rn(pj.y, pl.y), g.rp_pattern);
-    if (!(rp3 < g.sqr_rpmax && rp3 > g.sqr_rpmin)) return;
+    if (!(dlt_pos(rp3, g.sqr_rpmax) && dlt_pos(g.sqr_rpmin, rp3))) return;
     idx = rppi_index(abj.x, abl.x, rp3, abj.y, abl.y, pi3, sb, g.nb, g.npi);
     if (idx < 0) return;
     if (WEIGHTED) w = __dmul_rn(__dmul_rn(p1.w, pj.w), pl.w);
     if (SYM) {
       // The (l, j) ordering: same sides, anchor sides swapped.
-      if (abj.x == abl.x || abj.x == rp3 || abl.x == rp3)
+      if (deq_pos(abj.x, abl.x) || deq_pos(abj.x, rp3) || deq_pos(abl.x, rp3))
         idx2 = rppi_index(abl.x, abj.x, rp3, abl.y, abj.y, pi3, sb, g.nb, g.npi);
       else
         idx2 = idx;
@@ -434,7 +449,7 @@ __device__ __forceinline__ void rppi_exact_pair(const RppiArgs& a, const RppiOut
     }
   } else {
     const double s3 = sqr_sep_exact(pj.x, pj.y, pj.z, pl.x, pl.y, pl.z, g.fma_pattern);
-    if (!(s3 < g.sqr_rmax && s3 > g.sqr_rmin)) return;
+    if (!(dlt_pos(s3, g.sqr_rmax) && dlt_pos(g.sqr_rmin, s3))) return;
     // getLOS (source/device.cu:45-56): positions relative to d_ori, summed
     // left to right.
     const double lx = __dadd_rn(__dadd_rn(o1x, __dsub_rn(pj.x, g.ori_x)), __dsub_rn(pl.x, g.ori_x));
@@ -446,18 +461,20 @@ __device__ __forceinline__ void rppi_exact_pair(const RppiArgs& a, const RppiOut
     double t = dot3_exact(lx, ly, lz, __dsub_rn(p1.x, pj.x), __dsub_rn(p1.y, pj.y), __dsub_rn(p1.z, pj.z),
                           g.dot_pattern);
     const double q1 = __dmul_rn(t, t);
-    if (pm < q1) return;
+    if (dlt_pos(pm, q1)) return;
     t = dot3_exact(lx, ly, lz, __dsub_rn(p1.x, pl.x), __dsub_rn(p1.y, pl.y), __dsub_rn(p1.z, pl.z), g.dot_pattern);
     const double q2 = __dmul_rn(t, t);
-    if (pm < q2) return;
+    if (dlt_pos(pm, q2)) return;
     t = dot3_exact(lx, ly, lz, __dsub_rn(pj.x, pl.x), __dsub_rn(pj.y, pl.y), __dsub_rn(pj.z, pl.z), g.dot_pattern);
     const double q3 = __dmul_rn(t, t);
-    if (pm < q3) return;
+    if (dlt_pos(pm, q3)) return;
     // getSqrRpSqrPi (source/device.cu:65-68).
     const double pi1 = __ddiv_rn(q1, sqrL), pi2 = __ddiv_rn(q2, sqrL), pi3 = __ddiv_rn(q3, sqrL);
     const double rp1 = __dsub_rn(abj.x, pi1), rp2 = __dsub_rn(abl.x, pi2), rp3 = __dsub_rn(s3, pi3);
-    if (!(rp1 < g.sqr_rpmax && rp2 < g.sqr_rpmax && rp3 < g.sqr_rpmax && rp1 > g.sqr_rpmin &&
-          rp2 > g.sqr_rpmin && rp3 > g.sqr_rpmin && pi1 < g.sqr_pimax && pi2 < g.sqr_pimax))
+    // rp may round below zero; the limits are rpMax^2 > 0 and rpMin^2 >= 0.
+    if (!(dlt_lim(rp1, g.sqr_rpmax) && dlt_lim(rp2, g.sqr_rpmax) && dlt_lim(rp3, g.sqr_rpmax) &&
+          dgt_lim(rp1, g.sqr_rpmin) && dgt_lim(rp2, g.sqr_rpmin) && dgt_lim(rp3, g.sqr_rpmin) &&
+          dlt_pos(pi1, g.sqr_pimax) && dlt_pos(pi2, g.sqr_pimax)))
       return;
     idx = rppi_index(rp1, rp2, rp3, pi1, pi2, pi3, sb, g.nb, g.npi);
     if (WEIGHTED) w = __dmul_rn(__dmul_rn(p1.w, pj.w), pl.w);
