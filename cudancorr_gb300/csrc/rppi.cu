@@ -343,7 +343,8 @@ __device__ __forceinline__ int rppi_settle(const RppiArgs& a, const double4_16a&
       // The anchor-relative offset fl32(q - p1) = -fl32(p1 - q) and, in a
       // box, the classifier's per-side inputs: sqrt_rn(fl32(rp^2)) and the
       // exact rp and pi bins (floor(sqrtf(pi^2)) as the reference forms it).
-      const float rho = SURVEY ? 0.0f : __fsqrt_rn(__double2float_rn(x));
+      // (Survey: .w holds fl32(s^2) for rppi_survey_pair_cut.)
+      const float rho = SURVEY ? __double2float_rn(x) : __fsqrt_rn(__double2float_rn(x));
       L.rel[k] = make_float4(-__double2float_rn(dx), -__double2float_rn(dy), -__double2float_rn(dz), rho);
       if (!SURVEY)
         L.meta[k] = static_cast<unsigned>(exact_bin_pos(x, sb, g.nb)) |
@@ -556,7 +557,11 @@ __global__ void __launch_bounds__(kRppiThreads) k_rppi(const __grid_constant__ R
     __syncwarp();  // the lists are complete
     // Phase B.
     double o1x = 0.0;
-    if (SURVEY) o1x = __dsub_rn(p1.x, g.ori_x);  // pos1 = p1 - d_ori, d_ori = (ori.x, 0, 0)
+    float4 los = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (SURVEY) {
+      o1x = __dsub_rn(p1.x, g.ori_x);  // pos1 = p1 - d_ori, d_ori = (ori.x, 0, 0)
+      los = make_float4(__double2float_rn(o1x), __double2float_rn(p1.y), __double2float_rn(p1.z), 0.0f);
+    }
     constexpr bool kTri = SYM && !SURVEY;  // pairs j < l
     int j = 0, l = kTri ? 1 + lane : lane;
     rppi_norm<kTri>(j, l, n2, n3);
@@ -593,7 +598,8 @@ __global__ void __launch_bounds__(kRppiThreads) k_rppi(const __grid_constant__ R
         unc = vc && fi == kRppiUncertain;
       } else {
         const float dxf = rj.x - rl.x, dyf = rj.y - rl.y, dzf = rj.z - rl.z;
-        unc = vc && fmaf(dzf, dzf, fmaf(dxf, dxf, dyf * dyf)) <= g.f_s_hi;
+        unc = vc && fmaf(dzf, dzf, fmaf(dxf, dxf, dyf * dyf)) <= g.f_s_hi &&
+              !rppi_survey_pair_cut(rj, rl, los, g.los_smax, g.fast.pimax2, g.fast.rpmax2_hi, g.fast.rpmin2_lo);
       }
       const unsigned m = __ballot_sync(kRppiFull, unc);
       if (unc) ws.ring[(tail + __popc(m & lt)) & (kRppiRing - 1)] = make_int2(j, l);

@@ -161,6 +161,53 @@ __host__ __device__ inline bool rppi_los_cut(float dx, float dy, float dz, float
          (hi * (1.0f - cmin * cmin) + 1e-5f * hi <= rpmin2 * (1.0f - 1e-5f));
 }
 
+// Survey mode: whether the pair (j, l) of an anchor's list is certainly not
+// counted, from FP32 estimates of the reference's line-of-sight projections
+// (getLOS, getSqrSdotL, getSqrRpSqrPi, source/device.cu:45-68, and the tests
+// at :470-490). Inputs: the FP32 offsets dj = pj - p1 and dl = pl - p1 with
+// their FP32 s^2 in .w, and A = (p1.x - ori.x, p1.y, p1.z) in FP32. The
+// line of sight is L = 3A + dj + dl; tau_k = L.d_k / |L| is side k's
+// projection (d1 = dj, d2 = dl, d3 = dj - dl), pi_k = tau_k^2 and rp_k =
+// s_k^2 - pi_k. With u = 2^-24, each offset errs by u|d| and each A
+// component by u|A|, so the FP32 L is within EL = 4u(|L| + 8 sMax) of the
+// true one, and tau_k within |d_k| (4 EL / |L| + 16u) + 8u sMax; s3^2 from
+// the FP32 d3 within 32u sMax^2. The pair is rejected when, over those
+// ranges, a pi_k (k = 1, 2, 3) certainly exceeds piMax^2 or an rp_k certainly
+// lies outside (rpMin^2, rpMax^2); the reference rejects it then, whatever
+// its FP64 rounding (a further relative 1e-6 margin). los = (A, |A|); smax
+// >= sMax; pimax2, rpmax2 >= and rpmin2 <= the squared limits.
+__host__ __device__ inline bool rppi_survey_pair_cut(float4 dj, float4 dl, float4 los, float smax, float pimax2,
+                                                     float rpmax2, float rpmin2) {
+  const float u = 5.9604645e-8f;  // 2^-24
+  const float lx = fmaf(3.0f, los.x, dj.x + dl.x), ly = fmaf(3.0f, los.y, dj.y + dl.y),
+              lz = fmaf(3.0f, los.z, dj.z + dl.z);
+  const float ln = sqrtf(fmaf(lz, lz, fmaf(ly, ly, lx * lx)));
+  const float el = 4.0f * u * (ln + 8.0f * smax);
+  if (!(ln > 2.0f * el)) return false;
+  const float inv = 1.0f / ln, ang = 4.0f * el / (ln - el) + 16.0f * u, ed = 8.0f * u * smax;
+  const float d3x = dj.x - dl.x, d3y = dj.y - dl.y, d3z = dj.z - dl.z;
+  const float s3 = fmaf(d3z, d3z, fmaf(d3y, d3y, d3x * d3x));
+  const float t1 = fabsf(fmaf(lz, dj.z, fmaf(ly, dj.y, lx * dj.x))) * inv;
+  const float t2 = fabsf(fmaf(lz, dl.z, fmaf(ly, dl.y, lx * dl.x))) * inv;
+  const float t3 = fabsf(fmaf(lz, d3z, fmaf(ly, d3y, lx * d3x))) * inv;
+  const float e1 = sqrtf(dj.w) * ang + ed, e2 = sqrtf(dl.w) * ang + ed, e3 = sqrtf(s3) * ang + 2.0f * ed;
+  const float es3 = 32.0f * u * smax * smax;
+  const float pm = pimax2 * (1.0f + 1e-6f), rhi = rpmax2 * (1.0f + 1e-6f), rlo = rpmin2 * (1.0f - 1e-6f);
+  // Lower and upper bounds of tau_k^2, and of s_k^2.
+  const float a1 = fmaxf(t1 - e1, 0.0f), a2 = fmaxf(t2 - e2, 0.0f), a3 = fmaxf(t3 - e3, 0.0f);
+  const float b1 = t1 + e1, b2 = t2 + e2, b3 = t3 + e3;
+  const float sl1 = dj.w * (1.0f - 4.0f * u), sl2 = dl.w * (1.0f - 4.0f * u), sl3 = s3 - es3;
+  const float sh1 = dj.w * (1.0f + 4.0f * u), sh2 = dl.w * (1.0f + 4.0f * u), sh3 = s3 + es3;
+  const bool pi_out = (a1 * a1 > pm) | (a2 * a2 > pm) | (a3 * a3 > pm);
+  const bool rp_hi = (sl1 - b1 * b1 - 1e-6f * (sl1 + b1 * b1) > rhi) |
+                     (sl2 - b2 * b2 - 1e-6f * (sl2 + b2 * b2) > rhi) |
+                     (sl3 - b3 * b3 - 1e-6f * (fabsf(sl3) + b3 * b3) > rhi);
+  const bool rp_lo = ((sh1 - a1 * a1) * (1.0f + 1e-6f) + 1e-6f * sh1 < rlo) |
+                     ((sh2 - a2 * a2) * (1.0f + 1e-6f) + 1e-6f * sh2 < rlo) |
+                     ((sh3 - a3 * a3) * (1.0f + 1e-6f) + 1e-6f * sh3 < rlo);
+  return pi_out | rp_hi | rp_lo;
+}
+
 // An estimate of sqrt(x) for x >= 0; its error only costs certainty (the
 // pi-bin test below checks the bin it gives against margins).
 __host__ __device__ inline float rppi_sqrt_est(float x) {
