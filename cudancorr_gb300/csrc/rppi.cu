@@ -343,7 +343,7 @@ __device__ __forceinline__ int rppi_settle(const RppiArgs& a, const double4_16a&
       // The anchor-relative offset fl32(q - p1) = -fl32(p1 - q) and, in a
       // box, the classifier's per-side inputs: sqrt_rn(fl32(rp^2)) and the
       // exact rp and pi bins (floor(sqrtf(pi^2)) as the reference forms it).
-      // (Survey: .w holds fl32(s^2) for rppi_survey_pair_cut.)
+      // (Survey: .w holds fl32(s^2) for rppi_survey_index.)
       const float rho = SURVEY ? __double2float_rn(x) : __fsqrt_rn(__double2float_rn(x));
       L.rel[k] = make_float4(-__double2float_rn(dx), -__double2float_rn(dy), -__double2float_rn(dz), rho);
       if (!SURVEY)
@@ -507,9 +507,8 @@ __global__ void __launch_bounds__(kRppiThreads) k_rppi(const __grid_constant__ R
   __shared__ __align__(16) unsigned char s_tab[kRppiTab];
   __shared__ RppiWarpSm s_w[kRppiWarps];
   for (int i = threadIdx.x; i <= g.nb; i += blockDim.x) s_sb[i] = g.sqr_bins[i];
-  if (!SURVEY)
-    for (int i = threadIdx.x; i < kRppiTab / 16; i += blockDim.x)
-      reinterpret_cast<uint4*>(s_tab)[i] = reinterpret_cast<const uint4*>(a.tab)[i];
+  for (int i = threadIdx.x; i < kRppiTab / 16; i += blockDim.x)
+    reinterpret_cast<uint4*>(s_tab)[i] = reinterpret_cast<const uint4*>(a.tab)[i];
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const unsigned lt = (1u << lane) - 1u;
@@ -576,31 +575,33 @@ __global__ void __launch_bounds__(kRppiThreads) k_rppi(const __grid_constant__ R
     for (;;) {
       if (!__any_sync(kRppiFull, valid)) break;
       const bool vc = (SYM && SURVEY) ? valid && j != l : valid;
-      bool unc;
+      // FP32 classification (rppi_fast_index in a box, rppi_survey_index in a
+      // survey after the FP32 s^2 prefilter); the FP64 restatement settles
+      // what it leaves uncertain.
+      bool pre = vc;
+      int fi;
       if (!SURVEY) {
-        // FP32 classification; the FP64 restatement settles what it leaves
-        // uncertain.
-        const int fi = rppi_fast_index(rj.x, rj.y, rj.z, rj.w, mj, rl.x, rl.y, rl.z, rl.w, ml, g.fast,
-                                       s_tab);
-        const bool hit = vc && fi >= 0;
-        n_fast += hit ? 1u : 0u;
-        if (WEIGHTED) {
-          if (hit) {
-            const double w = __dmul_rn(L2.pw[jj], L3.pos[ll].w);   // (w1 w2) w3
-            const double w2 = __dmul_rn(L3.pw[ll], L2.pos[jj].w);  // (w1 w3) w2
-            rppi_count<SURVEY, SYM, WEIGHTED>(out, fi, fi, w, w2);  // no rp^2 ties when certain
-          }
-        } else {
-          // One count per ordering (two when p2 == p3: no rp^2 ties when
-          // certain); indices past the histogram go to its overflow slot.
-          rppi_red_u64(hit, out.u + min(max(fi, 0), nbins32), SYM ? 2ull : 1ull);
-        }
-        unc = vc && fi == kRppiUncertain;
+        fi = rppi_fast_index(rj.x, rj.y, rj.z, rj.w, mj, rl.x, rl.y, rl.z, rl.w, ml, g.fast, s_tab);
       } else {
         const float dxf = rj.x - rl.x, dyf = rj.y - rl.y, dzf = rj.z - rl.z;
-        unc = vc && fmaf(dzf, dzf, fmaf(dxf, dxf, dyf * dyf)) <= g.f_s_hi &&
-              !rppi_survey_pair_cut(rj, rl, los, g.los_smax, g.fast.pimax2, g.fast.rpmax2_hi, g.fast.rpmin2_lo);
+        pre = pre && fmaf(dzf, dzf, fmaf(dxf, dxf, dyf * dyf)) <= g.f_s_hi;
+        fi = rppi_survey_index(rj, rl, los, g.los_smax, g.fast, s_tab);
       }
+      const bool hit = pre && fi >= 0;
+      n_fast += hit ? 1u : 0u;
+      if (WEIGHTED) {
+        if (hit) {
+          const double w = __dmul_rn(L2.pw[jj], L3.pos[ll].w);   // (w1 w2) w3
+          const double w2 = __dmul_rn(L3.pw[ll], L2.pos[jj].w);  // (w1 w3) w2, box with p2 == p3
+          rppi_count<SURVEY, SYM, WEIGHTED>(out, fi, fi, w, w2);  // no rp^2 ties when certain
+        }
+      } else {
+        // One count per ordering (two for a box pair when p2 == p3: no rp^2
+        // ties when certain); indices past the histogram go to its overflow
+        // slot.
+        rppi_red_u64(hit, out.u + min(max(fi, 0), nbins32), (SYM && !SURVEY) ? 2ull : 1ull);
+      }
+      const bool unc = pre && fi == kRppiUncertain;
       const unsigned m = __ballot_sync(kRppiFull, unc);
       if (unc) ws.ring[(tail + __popc(m & lt)) & (kRppiRing - 1)] = make_int2(j, l);
       tail += __popc(m);

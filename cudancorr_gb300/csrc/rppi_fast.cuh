@@ -161,53 +161,6 @@ __host__ __device__ inline bool rppi_los_cut(float dx, float dy, float dz, float
          (hi * (1.0f - cmin * cmin) + 1e-5f * hi <= rpmin2 * (1.0f - 1e-5f));
 }
 
-// Survey mode: whether the pair (j, l) of an anchor's list is certainly not
-// counted, from FP32 estimates of the reference's line-of-sight projections
-// (getLOS, getSqrSdotL, getSqrRpSqrPi, source/device.cu:45-68, and the tests
-// at :470-490). Inputs: the FP32 offsets dj = pj - p1 and dl = pl - p1 with
-// their FP32 s^2 in .w, and A = (p1.x - ori.x, p1.y, p1.z) in FP32. The
-// line of sight is L = 3A + dj + dl; tau_k = L.d_k / |L| is side k's
-// projection (d1 = dj, d2 = dl, d3 = dj - dl), pi_k = tau_k^2 and rp_k =
-// s_k^2 - pi_k. With u = 2^-24, each offset errs by u|d| and each A
-// component by u|A|, so the FP32 L is within EL = 4u(|L| + 8 sMax) of the
-// true one, and tau_k within |d_k| (4 EL / |L| + 16u) + 8u sMax; s3^2 from
-// the FP32 d3 within 32u sMax^2. The pair is rejected when, over those
-// ranges, a pi_k (k = 1, 2, 3) certainly exceeds piMax^2 or an rp_k certainly
-// lies outside (rpMin^2, rpMax^2); the reference rejects it then, whatever
-// its FP64 rounding (a further relative 1e-6 margin). los = (A, |A|); smax
-// >= sMax; pimax2, rpmax2 >= and rpmin2 <= the squared limits.
-__host__ __device__ inline bool rppi_survey_pair_cut(float4 dj, float4 dl, float4 los, float smax, float pimax2,
-                                                     float rpmax2, float rpmin2) {
-  const float u = 5.9604645e-8f;  // 2^-24
-  const float lx = fmaf(3.0f, los.x, dj.x + dl.x), ly = fmaf(3.0f, los.y, dj.y + dl.y),
-              lz = fmaf(3.0f, los.z, dj.z + dl.z);
-  const float ln = sqrtf(fmaf(lz, lz, fmaf(ly, ly, lx * lx)));
-  const float el = 4.0f * u * (ln + 8.0f * smax);
-  if (!(ln > 2.0f * el)) return false;
-  const float inv = 1.0f / ln, ang = 4.0f * el / (ln - el) + 16.0f * u, ed = 8.0f * u * smax;
-  const float d3x = dj.x - dl.x, d3y = dj.y - dl.y, d3z = dj.z - dl.z;
-  const float s3 = fmaf(d3z, d3z, fmaf(d3y, d3y, d3x * d3x));
-  const float t1 = fabsf(fmaf(lz, dj.z, fmaf(ly, dj.y, lx * dj.x))) * inv;
-  const float t2 = fabsf(fmaf(lz, dl.z, fmaf(ly, dl.y, lx * dl.x))) * inv;
-  const float t3 = fabsf(fmaf(lz, d3z, fmaf(ly, d3y, lx * d3x))) * inv;
-  const float e1 = sqrtf(dj.w) * ang + ed, e2 = sqrtf(dl.w) * ang + ed, e3 = sqrtf(s3) * ang + 2.0f * ed;
-  const float es3 = 32.0f * u * smax * smax;
-  const float pm = pimax2 * (1.0f + 1e-6f), rhi = rpmax2 * (1.0f + 1e-6f), rlo = rpmin2 * (1.0f - 1e-6f);
-  // Lower and upper bounds of tau_k^2, and of s_k^2.
-  const float a1 = fmaxf(t1 - e1, 0.0f), a2 = fmaxf(t2 - e2, 0.0f), a3 = fmaxf(t3 - e3, 0.0f);
-  const float b1 = t1 + e1, b2 = t2 + e2, b3 = t3 + e3;
-  const float sl1 = dj.w * (1.0f - 4.0f * u), sl2 = dl.w * (1.0f - 4.0f * u), sl3 = s3 - es3;
-  const float sh1 = dj.w * (1.0f + 4.0f * u), sh2 = dl.w * (1.0f + 4.0f * u), sh3 = s3 + es3;
-  const bool pi_out = (a1 * a1 > pm) | (a2 * a2 > pm) | (a3 * a3 > pm);
-  const bool rp_hi = (sl1 - b1 * b1 - 1e-6f * (sl1 + b1 * b1) > rhi) |
-                     (sl2 - b2 * b2 - 1e-6f * (sl2 + b2 * b2) > rhi) |
-                     (sl3 - b3 * b3 - 1e-6f * (fabsf(sl3) + b3 * b3) > rhi);
-  const bool rp_lo = ((sh1 - a1 * a1) * (1.0f + 1e-6f) + 1e-6f * sh1 < rlo) |
-                     ((sh2 - a2 * a2) * (1.0f + 1e-6f) + 1e-6f * sh2 < rlo) |
-                     ((sh3 - a3 * a3) * (1.0f + 1e-6f) + 1e-6f * sh3 < rlo);
-  return pi_out | rp_hi | rp_lo;
-}
-
 // An estimate of sqrt(x) for x >= 0; its error only costs certainty (the
 // pi-bin test below checks the bin it gives against margins).
 __host__ __device__ inline float rppi_sqrt_est(float x) {
@@ -218,6 +171,109 @@ __host__ __device__ inline float rppi_sqrt_est(float x) {
 #else
   return std::sqrt(x);
 #endif
+}
+
+// Survey mode: the FP32 classification of a pair (j, l) of an anchor's list:
+// the flat index when every decision of the reference (source/device.cu:
+// 455-490 and getTriangleIndexRppi, :203-255) is certain, -1 when it
+// certainly does not count the pair, and kRppiUncertain otherwise. Inputs:
+// the FP32 offsets dj = pj - p1 and dl = pl - p1 with their FP32 s^2 in .w,
+// and A = (p1.x - ori.x, p1.y, p1.z) in FP32. The reference's line of sight
+// (getLOS, getSqrSdotL, getSqrRpSqrPi, :45-68) is L = 3A + dj + dl; tau_k =
+// L.d_k / |L| is side k's projection (d1 = dj, d2 = dl, d3 = dj - dl), pi_k
+// = tau_k^2 and rp_k = s_k^2 - pi_k. With u = 2^-24, each offset errs by
+// u|d| and each A component by u|A|, so the FP32 L is within EL = 4u(|L| +
+// 8 sMax) of the true one, tau_k within |d_k| (4 EL / |L| + 16u) + 8u sMax,
+// and s3^2 from the FP32 d3 within 32u sMax^2; the bounds below add the FP32
+// rounding of their own evaluation and a relative 1e-6 that covers the
+// reference's FP64 rounding. Side k's rp^2 and pi^2 thus lie in intervals
+// [R_lo, R_hi] and [P_lo, P_hi]. The pair is certainly not counted when a
+// pi^2 exceeds piMax^2 or an rp^2 leaves (rpMin^2, rpMax^2) over its whole
+// interval. The decisions are certain when: s3^2 is inside
+// (0, sMax^2); every pi^2 is below piMax^2 and every rp^2 inside (rpMin^2,
+// rpMax^2); the three rp^2 intervals are disjoint (their order is the
+// reference's sort; ties are never certain); sqrt(R_lo) of the two shortest
+// sides exceed sqrt(R_hi) of the longest by a relative 1e-6 (the FP32 sqrtf
+// test keeps the triangle); every rp^2 interval lies in one bin of the rp^2
+// table, whose cells decide a bin only for all values within f.erp of them
+// (so the interval's half-width must not exceed f.erp); and the pi^2
+// intervals of the two shortest sides lie farther than f.pmarg from the
+// squares k^2, (k+1)^2 around their pi bin k, which covers the FP32 rounding
+// of the reference's floor(sqrtf(pi^2)).
+__host__ __device__ inline int rppi_survey_index(float4 dj, float4 dl, float4 los, float smax, const RppiFast& f,
+                                                 const unsigned char* tab) {
+  const float u = 5.9604645e-8f;  // 2^-24
+  const float lx = fmaf(3.0f, los.x, dj.x + dl.x), ly = fmaf(3.0f, los.y, dj.y + dl.y),
+              lz = fmaf(3.0f, los.z, dj.z + dl.z);
+  const float ln = sqrtf(fmaf(lz, lz, fmaf(ly, ly, lx * lx)));
+  const float el = 4.0f * u * (ln + 8.0f * smax);
+  if (!(ln > 2.0f * el)) return kRppiUncertain;
+  const float inv = 1.0f / ln, ang = 4.0f * el / (ln - el) + 16.0f * u, ed = 8.0f * u * smax;
+  const float d3x = dj.x - dl.x, d3y = dj.y - dl.y, d3z = dj.z - dl.z;
+  const float s3 = fmaf(d3z, d3z, fmaf(d3y, d3y, d3x * d3x));
+  const float t[3] = {fabsf(fmaf(lz, dj.z, fmaf(ly, dj.y, lx * dj.x))) * inv,
+                      fabsf(fmaf(lz, dl.z, fmaf(ly, dl.y, lx * dl.x))) * inv,
+                      fabsf(fmaf(lz, d3z, fmaf(ly, d3y, lx * d3x))) * inv};
+  const float ss[3] = {dj.w, dl.w, s3};
+  const float es3 = 32.0f * u * smax * smax;
+  const float pm = f.pimax2 * (1.0f + 1e-6f), pml = f.pimax2 * (1.0f - 1e-6f);
+  const float rhi = f.rpmax2_hi * (1.0f + 1e-6f), rhl = f.rpmax2_lo * (1.0f - 1e-6f);
+  const float rlo = f.rpmin2_lo * (1.0f - 1e-6f), rll = f.rpmin2_hi * (1.0f + 1e-6f);
+  float plo[3], phi[3], rl[3], rh[3];
+  bool reject = false, ok = true;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float e = sqrtf(ss[k]) * ang + (k == 2 ? 2.0f : 1.0f) * ed;
+    const float a = fmaxf(t[k] - e, 0.0f), b = t[k] + e;
+    const float sl = k == 2 ? ss[k] - es3 : ss[k] * (1.0f - 4.0f * u);
+    const float sh = k == 2 ? ss[k] + es3 : ss[k] * (1.0f + 4.0f * u);
+    plo[k] = a * a * (1.0f - 4.0f * u);
+    phi[k] = b * b * (1.0f + 4.0f * u);
+    rl[k] = sl - phi[k] - 1e-6f * (fabsf(sl) + phi[k]);
+    rh[k] = sh - plo[k] + 1e-6f * (sh + plo[k]);
+    reject |= (plo[k] > pm) | (rl[k] > rhi) | (rh[k] < rlo);
+    ok &= (phi[k] < pml) & (rh[k] < rhl) & (rl[k] > rll);
+  }
+  ok &= (s3 + es3 < f.rpmax2_lo + f.pimax2 * (1.0f - 1e-6f)) & (s3 - es3 > 0.0f);
+  // The reference's sort of (rp1, rp2, rp3): certain when the intervals are
+  // disjoint. o[i] = the side in sorted position i.
+  const bool g01 = rl[0] > rh[1], l01 = rh[0] < rl[1];
+  const bool g02 = rl[0] > rh[2], l02 = rh[0] < rl[2];
+  const bool g12 = rl[1] > rh[2], l12 = rh[1] < rl[2];
+  ok &= (g01 | l01) & (g02 | l02) & (g12 | l12);
+  // Rank of sides 0 and 1 (number of sides below; side 2 takes the rest).
+  const int rk0 = (g01 ? 1 : 0) + (g02 ? 1 : 0), rk1 = (l01 ? 1 : 0) + (g12 ? 1 : 0);
+  auto side_at = [&](int r) { return rk0 == r ? 0 : (rk1 == r ? 1 : 2); };
+  const int oa = side_at(0), ob = side_at(1), oc = side_at(2);
+  // Side k's values by selects (no indexed register arrays).
+  auto pick = [](const float* v, int k) { return k == 0 ? v[0] : (k == 1 ? v[1] : v[2]); };
+  // FP32 triangle test of the sorted sides: keep certain.
+  ok &= (sqrtf(fmaxf(pick(rl, oa), 0.0f)) + sqrtf(fmaxf(pick(rl, ob), 0.0f))) * (1.0f - 1e-6f) >
+        sqrtf(fmaxf(pick(rh, oc), 0.0f)) * (1.0f + 1e-6f);
+  // rp bins from the table, pi bins of the two shortest sides.
+  int bin[3], pib[2];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const int k = i == 0 ? oa : (i == 1 ? ob : oc);
+    const float rlk = pick(rl, k), rhk = pick(rh, k), plk = pick(plo, k), phk = pick(phi, k);
+    const float mid = 0.5f * (rlk + rhk), hw = 0.5f * (rhk - rlk);
+    const int code = tab[static_cast<int>(fminf(fmaxf(mid, 0.0f) * f.tab_scale, static_cast<float>(kRppiTab - 1)))];
+    ok &= (code < kRppiTabReject) & (hw + 4.0f * u * fabsf(mid) <= f.erp);
+    bin[i] = code;
+    if (i < 2) {
+      const float pmid = 0.5f * (plk + phk);
+      const int q = static_cast<int>(fminf(rppi_sqrt_est(pmid), 4095.0f));
+      const float q2 = static_cast<float>(q * q), q3 = static_cast<float>((q + 1) * (q + 1));
+      ok &= ((q == 0) | (plk - f.pmarg > q2)) & (phk + f.pmarg < q3);
+      pib[i] = q;
+    }
+  }
+  const unsigned P = static_cast<unsigned>(f.npi), B = static_cast<unsigned>(f.nb);
+  const unsigned idx = static_cast<unsigned>(pib[1]) +
+                       P * (static_cast<unsigned>(pib[0]) +
+                            P * (static_cast<unsigned>(bin[2]) +
+                                 B * (static_cast<unsigned>(bin[1]) + B * static_cast<unsigned>(bin[0]))));
+  return reject ? -1 : (ok ? static_cast<int>(idx) : kRppiUncertain);
 }
 
 // The flat index (below 2^31: the constructor checks nb^3 nPi^2 + nPi), -1

@@ -12,8 +12,8 @@
 // tested against the reference's anchor-side test with partners that tilt
 // the line of sight as far as the list allows.
 //   rppi_gather_check <n_per_kind> <seed>
-// Survey pairs rejected by rppi_survey_pair_cut are checked against the
-// reference's full pair test.
+// Survey pairs that rppi_survey_index rejects or indexes are checked against
+// the reference's full pair test and index.
 // prints the counts of each part ("... violations <v> ... los_violations <w>
 // ... pair_violations <x>") and exits 1 on a violation.
 #include <cmath>
@@ -262,11 +262,14 @@ int main(int argc, char** argv) {
       }
     }
   }
-  // The survey pair cut (rppi_survey_pair_cut): every pair it rejects must
-  // fail the reference's FP64 survey test (source/device.cu:455-490).
-  long pair_checked = 0, pair_cut = 0, pair_near = 0, pair_violations = 0;
+  // The survey pair classifier (rppi_survey_index): a pair it rejects must
+  // not be counted by the reference (source/device.cu:455-490), and a pair
+  // it indexes must be counted at that index (getTriangleIndexRppi,
+  // :203-255, restated below in FP64).
+  long pair_checked = 0, pair_cut = 0, pair_idx = 0, pair_near = 0, pair_violations = 0;
   {
     const double rpmin = 2.0, rpmax = 30.0, pimax = 20.0;
+    const int nb = 8, npi = 20;
     const double sqr_rpmin = rpmin * rpmin, sqr_rpmax = rpmax * rpmax, sqr_pimax = pimax * pimax;
     const double sqr_rmax = sqr_rpmax + sqr_pimax, smax = std::sqrt(sqr_rmax);
     auto up = [](double x) {
@@ -277,8 +280,33 @@ int main(int argc, char** argv) {
       float f = static_cast<float>(x);
       return static_cast<double>(f) > x ? std::nextafter(f, -INFINITY) : f;
     };
-    const float smax_f = up(smax), pimax2_f = static_cast<float>(sqr_pimax), rpmax2_f = up(sqr_rpmax),
-                rpmin2_f = down(sqr_rpmin);
+    double edges[nb + 1], sb[nb + 1];
+    for (int i = 0; i <= nb; ++i) {
+      edges[i] = std::pow(10.0, std::log10(rpmin) + i * (std::log10(rpmax) - std::log10(rpmin)) / nb);
+      sb[i] = edges[i] * edges[i];
+    }
+    const double u = std::ldexp(1.0, -24);
+    ncorr_gb300::RppiFast f;
+    f.epi = up(64.0 * u * sqr_pimax);
+    f.erp = up(128.0 * u * sqr_rpmax);
+    f.pimax2 = static_cast<float>(sqr_pimax);
+    f.rpmax2_lo = down(sqr_rpmax);
+    f.rpmax2_hi = up(sqr_rpmax);
+    f.rpmin2_lo = down(sqr_rpmin);
+    f.rpmin2_hi = up(sqr_rpmin);
+    f.hm = -up(128.0 * u * sqr_rpmax);
+    f.pmarg = up(16.0 * u * sqr_pimax);
+    f.nb = nb;
+    f.npi = npi;
+    float e2lo[nb + 1], e2hi[nb + 1];
+    for (int i = 0; i <= nb; ++i) {
+      e2lo[i] = down(sb[i]);
+      e2hi[i] = up(sb[i]);
+    }
+    f.tab_scale = ncorr_gb300::rppi_tab_scale(f.rpmax2_hi, f.erp);
+    static unsigned char tab[ncorr_gb300::kRppiTab];
+    ncorr_gb300::rppi_build_table(f, e2lo, e2hi, tab);
+    const float smax_f = up(smax);
     auto dot = [](const double a[3], const double b[3]) { return std::fma(a[2], b[2], std::fma(a[0], b[0], a[1] * b[1])); };
     auto sep = [&](const double a[3], const double b[3]) {
       const double d[3] = {a[0] - b[0], a[1] - b[1], a[2] - b[2]};
@@ -288,6 +316,12 @@ int main(int argc, char** argv) {
       const double n = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
       for (int d = 0; d < 3; ++d) v[d] /= n;
     };
+    auto ebin = [&](double r) {
+      int b = 0;
+      for (int i = 1; i < nb; ++i)
+        if (r >= sb[i]) b = i;
+      return b;
+    };
     std::normal_distribution<double> N(0.0, 1.0);
     for (long it = 0; it < n_per_kind; ++it) {
       const double ori_x = (U(rng) - 0.5) * 200.0;
@@ -296,26 +330,27 @@ int main(int argc, char** argv) {
       const double an = 60.0 * std::pow(50.0, U(rng));
       const double p1[3] = {ori_x + an * dir[0], an * dir[1], an * dir[2]};
       const double A[3] = {p1[0] - ori_x, p1[1], p1[2]};
-      double e1[3] = {N(rng), N(rng), N(rng)}, e2[3];
+      double e1[3] = {N(rng), N(rng), N(rng)};
       const double ad = dot(e1, dir);
       for (int d = 0; d < 3; ++d) e1[d] -= ad * dir[d];
       unit(e1);
-      e2[0] = dir[1] * e1[2] - dir[2] * e1[1];
-      e2[1] = dir[2] * e1[0] - dir[0] * e1[2];
-      e2[2] = dir[0] * e1[1] - dir[1] * e1[0];
-      // pj and pl around p1; for kinds 0-2 the point is re-placed a few
-      // times against the pair's own line of sight L (which depends on it),
-      // until pi3, rp3 or pi1 lies on its limit to within 1e-6 relative.
-      const int kind = static_cast<int>(U(rng) * 4.0);
+      // pj and pl around p1; for kinds 0-6 a point is re-placed a few times
+      // against the pair's own line of sight L (which depends on it) until
+      // the chosen quantity sits on its limit to within 1e-6 relative: pi3,
+      // rp3 or pi1 on the cut, rp1 or rp3 on a bin edge, pi1 on an integer,
+      // or rp1 = rp2 exactly (pl the mirror image of pj across L).
+      const int kind = static_cast<int>(U(rng) * 8.0);
       const double eps = (U(rng) - 0.5) * 2e-6;
       auto rnd = [&](double r) { return (2.0 * U(rng) - 1.0) * r; };
       double pj[3], pl[3];
       for (int d = 0; d < 3; ++d) {
-        pj[d] = p1[d] + rnd(pimax) * dir[d] + rnd(rpmax * 0.7) * e1[d] + rnd(rpmax * 0.7) * e2[d];
-        pl[d] = p1[d] + rnd(smax * 0.57) * dir[d] + rnd(smax * 0.57) * e1[d] + rnd(smax * 0.57) * e2[d];
+        pj[d] = p1[d] + rnd(pimax) * dir[d] + rnd(rpmax * 0.7) * e1[d];
+        pl[d] = p1[d] + rnd(smax * 0.57) * dir[d] + rnd(smax * 0.57) * e1[d];
       }
       const double sgn = U(rng) < 0.5 ? -1.0 : 1.0, side = rnd(10.0), t0 = 2.0 * M_PI * U(rng);
-      for (int iter = 0; kind < 3 && iter < 6; ++iter) {
+      const double edge = edges[1 + static_cast<int>(U(rng) * (nb - 1))];
+      const double kpi = 1.0 + static_cast<int>(U(rng) * (pimax - 1.0));
+      for (int iter = 0; kind < 7 && iter < 8; ++iter) {
         double Lh[3] = {((p1[0] - ori_x) + (pj[0] - ori_x)) + (pl[0] - ori_x), (p1[1] + pj[1]) + pl[1],
                         (p1[2] + pj[2]) + pl[2]};
         unit(Lh);
@@ -325,13 +360,18 @@ int main(int argc, char** argv) {
         unit(f1);
         const double f2[3] = {Lh[1] * f1[2] - Lh[2] * f1[1], Lh[2] * f1[0] - Lh[0] * f1[2],
                               Lh[0] * f1[1] - Lh[1] * f1[0]};
-        if (kind == 0) {  // pi3 = piMax: pl = pj + piMax L^ + a sideways step
-          for (int d = 0; d < 3; ++d) pl[d] = pj[d] + sgn * pimax * (1.0 + eps) * Lh[d] + side * f1[d];
-        } else if (kind == 1) {  // rp3 = rpMax: pl = pj + a small step along L^ + rpMax across
-          for (int d = 0; d < 3; ++d)
-            pl[d] = pj[d] + side * Lh[d] + rpmax * (1.0 + eps) * (std::cos(t0) * f1[d] + std::sin(t0) * f2[d]);
-        } else {  // pi1 = piMax: pj = p1 + piMax L^ + a sideways step
-          for (int d = 0; d < 3; ++d) pj[d] = p1[d] + sgn * pimax * (1.0 + eps) * Lh[d] + side * f1[d];
+        const double cs = std::cos(t0), sn = std::sin(t0);
+        double dj[3];
+        for (int d = 0; d < 3; ++d) dj[d] = pj[d] - p1[d];
+        const double tj = dot(dj, Lh);
+        for (int d = 0; d < 3; ++d) {
+          if (kind == 0) pl[d] = pj[d] + sgn * pimax * (1.0 + eps) * Lh[d] + side * f1[d];
+          if (kind == 1) pl[d] = pj[d] + side * Lh[d] + rpmax * (1.0 + eps) * (cs * f1[d] + sn * f2[d]);
+          if (kind == 2) pj[d] = p1[d] + sgn * pimax * (1.0 + eps) * Lh[d] + side * f1[d];
+          if (kind == 3) pj[d] = p1[d] + side * Lh[d] + edge * (1.0 + eps) * (cs * f1[d] + sn * f2[d]);
+          if (kind == 4) pl[d] = pj[d] + side * Lh[d] + edge * (1.0 + eps) * (cs * f1[d] + sn * f2[d]);
+          if (kind == 5) pj[d] = p1[d] + sgn * kpi * (1.0 + eps) * Lh[d] + 0.5 * rpmax * (cs * f1[d] + sn * f2[d]);
+          if (kind == 6) pl[d] = p1[d] + tj * Lh[d] - (dj[d] - tj * Lh[d]);
         }
       }
       const double s1 = sep(p1, pj), s2 = sep(p1, pl);
@@ -343,11 +383,15 @@ int main(int argc, char** argv) {
       const float4 dl = {static_cast<float>(pl[0] - p1[0]), static_cast<float>(pl[1] - p1[1]),
                          static_cast<float>(pl[2] - p1[2]), static_cast<float>(s2)};
       const float4 los = {static_cast<float>(A[0]), static_cast<float>(A[1]), static_cast<float>(A[2]), 0.0f};
-      if (!ncorr_gb300::rppi_survey_pair_cut(dj, dl, los, smax_f, pimax2_f, rpmax2_f, rpmin2_f)) continue;
-      ++pair_cut;
-      pair_near += kind < 3;
-      // The reference's decision for (p1, pj, pl).
-      bool counted = false;
+      const int got = ncorr_gb300::rppi_survey_index(dj, dl, los, smax_f, f, tab);
+      if (got == ncorr_gb300::kRppiUncertain) continue;
+      if (got < 0)
+        ++pair_cut;
+      else
+        ++pair_idx;
+      pair_near += kind < 7;
+      // The reference's decision and index for (p1, pj, pl).
+      long long ref = -1;
       const double s3 = sep(pj, pl);
       if (s3 < sqr_rmax && s3 > 0.0) {
         const double L[3] = {((p1[0] - ori_x) + (pj[0] - ori_x)) + (pl[0] - ori_x), (p1[1] + pj[1]) + pl[1],
@@ -358,23 +402,37 @@ int main(int argc, char** argv) {
         const double d3[3] = {pj[0] - pl[0], pj[1] - pl[1], pj[2] - pl[2]};
         const double q1 = dot(L, d1) * dot(L, d1), q2 = dot(L, d2) * dot(L, d2), q3 = dot(L, d3) * dot(L, d3);
         if (!(pm < q1) && !(pm < q2) && !(pm < q3)) {
-          const double pi1 = q1 / sqrL, pi2 = q2 / sqrL, pi3 = q3 / sqrL;
-          const double rp1 = s1 - pi1, rp2 = s2 - pi2, rp3 = s3 - pi3;
-          counted = rp1 < sqr_rpmax && rp2 < sqr_rpmax && rp3 < sqr_rpmax && rp1 > sqr_rpmin && rp2 > sqr_rpmin &&
-                    rp3 > sqr_rpmin && pi1 < sqr_pimax && pi2 < sqr_pimax;
+          double qq[3] = {q1 / sqrL, q2 / sqrL, q3 / sqrL};
+          double rr[3] = {s1 - qq[0], s2 - qq[1], s3 - qq[2]};
+          if (rr[0] < sqr_rpmax && rr[1] < sqr_rpmax && rr[2] < sqr_rpmax && rr[0] > sqr_rpmin &&
+              rr[1] > sqr_rpmin && rr[2] > sqr_rpmin && qq[0] < sqr_pimax && qq[1] < sqr_pimax) {
+            double t;
+            if (rr[0] > rr[1]) { t = rr[0]; rr[0] = rr[1]; rr[1] = t; t = qq[0]; qq[0] = qq[1]; qq[1] = t; }
+            if (rr[0] > rr[2]) { t = rr[0]; rr[0] = rr[2]; rr[2] = t; t = qq[0]; qq[0] = qq[2]; qq[2] = t; }
+            if (rr[1] > rr[2]) { t = rr[1]; rr[1] = rr[2]; rr[2] = t; t = qq[1]; qq[1] = qq[2]; qq[2] = t; }
+            const float r1 = std::sqrt(static_cast<float>(rr[0])), r2 = std::sqrt(static_cast<float>(rr[1])),
+                        r3 = std::sqrt(static_cast<float>(rr[2]));
+            if (!(r1 + r2 <= r3)) {
+              const long long P = npi, B = nb;
+              const long long p1b = static_cast<long long>(std::floor(std::sqrt(static_cast<float>(qq[0]))));
+              const long long p2b = static_cast<long long>(std::floor(std::sqrt(static_cast<float>(qq[1]))));
+              ref = p2b + p1b * P + ebin(rr[2]) * P * P + ebin(rr[1]) * B * P * P + ebin(rr[0]) * B * B * P * P;
+            }
+          }
         }
       }
-      if (counted) {
+      if (static_cast<long long>(got) != ref) {
         if (pair_violations < 10)
-          std::printf("pair violation: kind %d A %.6g pj-p1 (%.9g %.9g %.9g) pl-p1 (%.9g %.9g %.9g)\n", kind, an,
-                      pj[0] - p1[0], pj[1] - p1[1], pj[2] - p1[2], pl[0] - p1[0], pl[1] - p1[1], pl[2] - p1[2]);
+          std::printf("pair violation: kind %d got %d ref %lld A %.6g pj-p1 (%.9g %.9g %.9g) pl-p1 (%.9g %.9g %.9g)\n",
+                      kind, got, ref, an, pj[0] - p1[0], pj[1] - p1[1], pj[2] - p1[2], pl[0] - p1[0], pl[1] - p1[1],
+                      pl[2] - p1[2]);
         ++pair_violations;
       }
     }
   }
   std::printf("checked %ld kept %ld dropped %ld near %ld violations %ld los_checked %ld los_cut %ld los_partners %ld "
-              "los_violations %ld pair_checked %ld pair_cut %ld pair_near %ld pair_violations %ld\n",
+              "los_violations %ld pair_checked %ld pair_cut %ld pair_idx %ld pair_near %ld pair_violations %ld\n",
               checked, kept, dropped, near, violations, los_checked, los_cut, los_partners, los_violations,
-              pair_checked, pair_cut, pair_near, pair_violations);
+              pair_checked, pair_cut, pair_idx, pair_near, pair_violations);
   return violations || los_violations || pair_violations ? 1 : 0;
 }

@@ -162,9 +162,10 @@ def test_rppi_gather_prefilter_never_drops_a_kept_point(tmp_path):
     face and through periodic images, in two boxes and a survey extent. Also
     the survey line-of-sight cut of list entries (rppi_los_cut): no entry it
     drops passes the reference's anchor-side test with any of its partners;
-    and the survey pair cut (rppi_survey_pair_cut): no pair it rejects, with
-    pi3, rp3 or pi1 on its limit against the pair's own line of sight, is
-    counted by the reference."""
+    and the survey pair classifier (rppi_survey_index): with pairs on the pi3,
+    rp3 and pi1 limits of their own line of sight, rp1 or rp3 on a bin edge,
+    pi1 on an integer and rp1 = rp2, every pair it rejects is not counted by
+    the reference and every pair it indexes is counted at that index."""
     import shutil
     import subprocess
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
@@ -180,7 +181,7 @@ def test_rppi_gather_prefilter_never_drops_a_kept_point(tmp_path):
         n = dict(zip(out.stdout.split()[0::2], map(int, out.stdout.split()[1::2])))
         assert n["violations"] == 0 and n["near"] > n["checked"] // 100 and n["kept"] > n["checked"] // 10
         assert n["los_violations"] == 0 and n["los_cut"] > n["los_checked"] // 10 and n["los_partners"] > 0
-        assert n["pair_violations"] == 0 and n["pair_near"] > n["pair_checked"] // 10
+        assert n["pair_violations"] == 0 and n["pair_near"] > n["pair_checked"] // 10 and n["pair_idx"] > 0
 
 
 def test_rppi_fp32_classifier_agrees_with_the_exact_computation(tmp_path):
