@@ -789,7 +789,8 @@ int rppi_init(ncorr_handle* h, const double box[3], const double* edges, int n_e
   f.pmarg = f32_up(16.0 * u * g.sqr_pimax);
   f.nb = nb;
   f.npi = num_minor_bins;
-  f.tab_scale = rppi_tab_scale(f.rpmax2_hi, f.erp);
+  f.tab_band = is_survey ? 4.0f * f.erp : f.erp;  // survey pairs carry wider bands than a box's third side
+  f.tab_scale = rppi_tab_scale(f.rpmax2_hi, f.tab_band);
   for (int i = 0; i < n_edges; ++i) {
     g.fe2lo[i] = f32_down(g.sqr_bins[i]);
     g.fe2hi[i] = f32_up(g.sqr_bins[i]);

@@ -40,6 +40,7 @@ struct RppiFast {
   float hm;                    // -M of the triangle margin
   float pmarg;                 // pi-bin margin
   float tab_scale;             // 2^k: entry of the rp3 table for an estimate rf
+  float tab_band;              // the table's band: erp in a box, 4 erp in a survey
   int nb, npi;
 };
 
@@ -47,29 +48,29 @@ constexpr int kRppiUncertain = -2;
 
 // The rp3 table: kRppiTab entries over the estimate rf of the third side's
 // rp^2, entry c for rf in [c, c + 1) / tab_scale (the last one for everything
-// above). An entry holds the bin b when every rf of its cell has
-// rf - erp > fl32 up(edge_b^2) and rf + erp < fl32 down(edge_{b+1}^2): the
-// reference's rp3 (within erp of rf) then lies in bin b, and so within
-// (rpMin^2, rpMax^2). It holds kRppiTabReject when every rf of the cell has
-// rf - erp >= rpmax2_hi or rf + erp < rpmin2_lo (rp3 certainly cut), else
+// above). With the band e = tab_band, an entry holds the bin b when every rf
+// of its cell has rf - e > fl32 up(edge_b^2) and rf + e < fl32
+// down(edge_{b+1}^2): an rp^2 within e of rf then lies in bin b, and so
+// within (rpMin^2, rpMax^2). It holds kRppiTabReject when every rf of the
+// cell has rf - e >= rpmax2_hi or rf + e < rpmin2_lo (certainly cut), else
 // kRppiTabUncertain. The bounds are evaluated exactly (in FP64, from FP32
 // inputs), and tab_scale is a power of two, so the kernel's cell index
 // floor(rf * tab_scale) is exact.
 constexpr int kRppiTab = 1 << 14;
 constexpr unsigned char kRppiTabReject = 0xFE, kRppiTabUncertain = 0xFF;
 
-inline float rppi_tab_scale(float rpmax2_hi, float erp) {
-  // The largest power of two with (kRppiTab - 1) / scale >= rpmax2_hi + erp,
+inline float rppi_tab_scale(float rpmax2_hi, float band) {
+  // The largest power of two with (kRppiTab - 1) / scale >= rpmax2_hi + band,
   // so that the last (clamped) entry is a reject.
-  const double need = (static_cast<double>(rpmax2_hi) + erp) / (kRppiTab - 1);
+  const double need = (static_cast<double>(rpmax2_hi) + band) / (kRppiTab - 1);
   return static_cast<float>(std::ldexp(1.0, -static_cast<int>(std::ceil(std::log2(need)))));
 }
 
 inline void rppi_build_table(const RppiFast& f, const float* e2lo, const float* e2hi, unsigned char* tab) {
   const double inv = 1.0 / f.tab_scale;
   for (int c = 0; c < kRppiTab; ++c) {
-    const double lo = c * inv - f.erp;  // infimum of rf - erp over the cell
-    const double hi = c == kRppiTab - 1 ? INFINITY : (c + 1) * inv + f.erp;  // supremum of rf + erp
+    const double lo = c * inv - f.tab_band;  // infimum of rf - band over the cell
+    const double hi = c == kRppiTab - 1 ? INFINITY : (c + 1) * inv + f.tab_band;  // supremum of rf + band
     unsigned char code = kRppiTabUncertain;
     if (lo >= f.rpmax2_hi || hi <= f.rpmin2_lo) {
       code = kRppiTabReject;
@@ -182,11 +183,15 @@ __host__ __device__ inline float rppi_sqrt_est(float x) {
 // (getLOS, getSqrSdotL, getSqrRpSqrPi, :45-68) is L = 3A + dj + dl; tau_k =
 // L.d_k / |L| is side k's projection (d1 = dj, d2 = dl, d3 = dj - dl), pi_k
 // = tau_k^2 and rp_k = s_k^2 - pi_k. With u = 2^-24, each offset errs by
-// u|d| and each A component by u|A|, so the FP32 L is within EL = 4u(|L| +
-// 8 sMax) of the true one, tau_k within |d_k| (4 EL / |L| + 16u) + 8u sMax,
-// and s3^2 from the FP32 d3 within 32u sMax^2; the bounds below add the FP32
-// rounding of their own evaluation and a relative 1e-6 that covers the
-// reference's FP64 rounding. Side k's rp^2 and pi^2 thus lie in intervals
+// u|d| and each A component by u|A|; the FP32 L = fl(fma(3, A, fl(dj + dl)))
+// is then within EL = u(2|L| + 6 sMax) of the true one (3|A| <= |L| + 2
+// sMax), its direction within 2 EL / |L|, and tau_k within |d_k| (2 EL / |L|
+// + 8u) + u sMax (4u sMax for d3 = fl(dj - dl)), the 8u covering the FP32
+// dot product and normalisation; s3^2 from the FP32 d3 is within 30u
+// sMax^2. The bounds carry 1% on these, 4u for the FP32 rounding of their
+// own evaluation, a factor 2 on EL and on the offset errors over this
+// derivation, and a relative 1e-6 on the limits that covers the reference's
+// FP64 rounding. Side k's rp^2 and pi^2 thus lie in intervals
 // [R_lo, R_hi] and [P_lo, P_hi]. The pair is certainly not counted when a
 // pi^2 exceeds piMax^2 or an rp^2 leaves (rpMin^2, rpMax^2) over its whole
 // interval. The decisions are certain when: s3^2 is inside
@@ -195,8 +200,8 @@ __host__ __device__ inline float rppi_sqrt_est(float x) {
 // reference's sort; ties are never certain); sqrt(R_lo) of the two shortest
 // sides exceed sqrt(R_hi) of the longest by a relative 1e-6 (the FP32 sqrtf
 // test keeps the triangle); every rp^2 interval lies in one bin of the rp^2
-// table, whose cells decide a bin only for all values within f.erp of them
-// (so the interval's half-width must not exceed f.erp); and the pi^2
+// table, whose cells decide a bin only for all values within f.tab_band of
+// them (so the interval's half-width must not exceed it); and the pi^2
 // intervals of the two shortest sides lie farther than f.pmarg from the
 // squares k^2, (k+1)^2 around their pi bin k, which covers the FP32 rounding
 // of the reference's floor(sqrtf(pi^2)).
@@ -206,16 +211,16 @@ __host__ __device__ inline int rppi_survey_index(float4 dj, float4 dl, float4 lo
   const float lx = fmaf(3.0f, los.x, dj.x + dl.x), ly = fmaf(3.0f, los.y, dj.y + dl.y),
               lz = fmaf(3.0f, los.z, dj.z + dl.z);
   const float ln = sqrtf(fmaf(lz, lz, fmaf(ly, ly, lx * lx)));
-  const float el = 4.0f * u * (ln + 8.0f * smax);
+  const float el = 2.02f * u * (2.0f * ln + 6.0f * smax);
   if (!(ln > 2.0f * el)) return kRppiUncertain;
-  const float inv = 1.0f / ln, ang = 4.0f * el / (ln - el) + 16.0f * u, ed = 8.0f * u * smax;
+  const float inv = 1.0f / ln, ang = 2.02f * el / (ln - el) + 8.0f * u, ed = 2.02f * u * smax;
   const float d3x = dj.x - dl.x, d3y = dj.y - dl.y, d3z = dj.z - dl.z;
   const float s3 = fmaf(d3z, d3z, fmaf(d3y, d3y, d3x * d3x));
   const float t[3] = {fabsf(fmaf(lz, dj.z, fmaf(ly, dj.y, lx * dj.x))) * inv,
                       fabsf(fmaf(lz, dl.z, fmaf(ly, dl.y, lx * dl.x))) * inv,
                       fabsf(fmaf(lz, d3z, fmaf(ly, d3y, lx * d3x))) * inv};
   const float ss[3] = {dj.w, dl.w, s3};
-  const float es3 = 32.0f * u * smax * smax;
+  const float es3 = 30.3f * u * smax * smax;
   const float pm = f.pimax2 * (1.0f + 1e-6f), pml = f.pimax2 * (1.0f - 1e-6f);
   const float rhi = f.rpmax2_hi * (1.0f + 1e-6f), rhl = f.rpmax2_lo * (1.0f - 1e-6f);
   const float rlo = f.rpmin2_lo * (1.0f - 1e-6f), rll = f.rpmin2_hi * (1.0f + 1e-6f);
@@ -223,14 +228,14 @@ __host__ __device__ inline int rppi_survey_index(float4 dj, float4 dl, float4 lo
   bool reject = false, ok = true;
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    const float e = sqrtf(ss[k]) * ang + (k == 2 ? 2.0f : 1.0f) * ed;
+    const float e = sqrtf(ss[k]) * ang + (k == 2 ? 4.0f : 1.0f) * ed;
     const float a = fmaxf(t[k] - e, 0.0f), b = t[k] + e;
     const float sl = k == 2 ? ss[k] - es3 : ss[k] * (1.0f - 4.0f * u);
     const float sh = k == 2 ? ss[k] + es3 : ss[k] * (1.0f + 4.0f * u);
     plo[k] = a * a * (1.0f - 4.0f * u);
     phi[k] = b * b * (1.0f + 4.0f * u);
-    rl[k] = sl - phi[k] - 1e-6f * (fabsf(sl) + phi[k]);
-    rh[k] = sh - plo[k] + 1e-6f * (sh + plo[k]);
+    rl[k] = sl - phi[k] - 4.0f * u * (fabsf(sl) + phi[k]);
+    rh[k] = sh - plo[k] + 4.0f * u * (sh + plo[k]);
     reject |= (plo[k] > pm) | (rl[k] > rhi) | (rh[k] < rlo);
     ok &= (phi[k] < pml) & (rh[k] < rhl) & (rl[k] > rll);
   }
@@ -258,7 +263,7 @@ __host__ __device__ inline int rppi_survey_index(float4 dj, float4 dl, float4 lo
     const float rlk = pick(rl, k), rhk = pick(rh, k), plk = pick(plo, k), phk = pick(phi, k);
     const float mid = 0.5f * (rlk + rhk), hw = 0.5f * (rhk - rlk);
     const int code = tab[static_cast<int>(fminf(fmaxf(mid, 0.0f) * f.tab_scale, static_cast<float>(kRppiTab - 1)))];
-    ok &= (code < kRppiTabReject) & (hw + 4.0f * u * fabsf(mid) <= f.erp);
+    ok &= (code < kRppiTabReject) & (hw + 4.0f * u * fabsf(mid) <= f.tab_band);
     bin[i] = code;
     if (i < 2) {
       const float pmid = 0.5f * (plk + phk);

@@ -99,7 +99,8 @@ int main(int argc, char** argv) {
     e2lo[i] = f32_down(sb[i]);
     e2hi[i] = f32_up(sb[i]);
   }
-  f.tab_scale = ncorr_gb300::rppi_tab_scale(f.rpmax2_hi, f.erp);
+  f.tab_band = f.erp;
+  f.tab_scale = ncorr_gb300::rppi_tab_scale(f.rpmax2_hi, f.tab_band);
   std::vector<unsigned char> tab(ncorr_gb300::kRppiTab);
   ncorr_gb300::rppi_build_table(f, e2lo.data(), e2hi.data(), tab.data());
 

@@ -303,7 +303,8 @@ int main(int argc, char** argv) {
       e2lo[i] = down(sb[i]);
       e2hi[i] = up(sb[i]);
     }
-    f.tab_scale = ncorr_gb300::rppi_tab_scale(f.rpmax2_hi, f.erp);
+    f.tab_band = 4.0f * f.erp;
+    f.tab_scale = ncorr_gb300::rppi_tab_scale(f.rpmax2_hi, f.tab_band);
     static unsigned char tab[ncorr_gb300::kRppiTab];
     ncorr_gb300::rppi_build_table(f, e2lo, e2hi, tab);
     const float smax_f = up(smax);
