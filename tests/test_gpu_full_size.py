@@ -11,7 +11,10 @@ kernel finish in seconds:
     shifted, 15 log bins in [5, 120): DDD, DDR, DRR and RRR unweighted, and
     weighted DDD/DDR/DRR against the FP64 oracle;
   * the batched mocks' largest catalogue (about 1M points, L=1000, r_max=60,
-    17 cells, the last 40 wide), inside a batch with three other mocks.
+    17 cells, the last 40 wide), inside a batch with three other mocks;
+  * the rppi bin type on the 2M-point clustered box and on the survey wedge
+    (rp 12 log bins in [1, 30), 30 unit pi bins): box, and survey DDD, DDR,
+    DRR against the oracle, survey DDD against the reference's rppi kernel.
 Against the CPU oracle the anchors are drawn at random. The reference kernel
 (source/device.cu:259-315, :381-431, compiled unmodified) runs one thread per
 anchor in FP64, so its time per anchor grows with (in-range neighbours) x
@@ -213,3 +216,57 @@ def test_largest_mock_reference_and_oracle_anchors(ref, engine_lib, mocks4):
     h_o = ref.count_threeD(box, edges, sub2, p, p)
     h2, _, _ = run_engine(box, edges, sub2, p, p)
     assert np.array_equal(h2, h_o)
+
+
+# --------------------------------------------------------------------------- rppi at the benchmark sizes
+def _rppi_run(box, edges, npi, p1, p2, p3, survey=False, ori=(0.0, 0.0, 0.0)):
+    from tests.test_gpu_rppi import run_rppi
+    h, st, _, _, _ = run_rppi(box, edges, npi, p1, p2, p3, survey=survey, ori=ori)
+    return h, st
+
+
+def test_rppi_box_clustered_2M_oracle_anchors(oracle, engine_lib):
+    """rppi on the 2M-point clustered box of the rppi benchmark (rp 12 log
+    bins in [1, 30), 30 unit pi bins), 4,096 random anchors against the
+    oracle: bit for bit, with the triangles past the histogram."""
+    p, box, _ = C.config_box_clustered(seed=2)
+    edges = api.logspace(1.0, 30.0, 13)
+    sub = random_anchors(p, 4096, 71)
+    t0 = time.perf_counter()
+    h_o, ov_o = oracle.count_rppi(box, edges, 30, sub, p, p)
+    print(f"\nrppi box 2M oracle: {len(sub)} anchors, {time.perf_counter() - t0:.1f} s")
+    h, st = _rppi_run(box, edges, 30, sub, p, p)
+    assert h_o.sum() > 0
+    assert np.array_equal(h, h_o) and st["overflow"] == ov_o
+
+
+@pytest.mark.parametrize("combo,n_anc", [("DDD", 2048), ("DDR", 512), ("DRR", 192)])
+def test_rppi_survey_full_oracle_anchors(oracle, engine_lib, survey_full, combo, n_anc):
+    """Survey-mode rppi (rp 12 log bins in [1, 30), 30 unit pi bins) on the
+    full wedge catalogues with unit weights, random anchors against the
+    oracle: bit for bit."""
+    s = survey_full
+    c1, c2, c3 = _survey_args(s, combo, True)
+    sub = random_anchors(c1, n_anc, 80 + n_anc)
+    edges = api.logspace(1.0, 30.0, 13)
+    t0 = time.perf_counter()
+    h_o, ov_o = oracle.count_rppi(s["box"], edges, 30, sub, c2, c3, survey=True, ori=s["ori"])
+    print(f"\nrppi survey {combo} oracle: {n_anc} anchors, {time.perf_counter() - t0:.1f} s")
+    h, st = _rppi_run(s["box"], edges, 30, sub, c2, c3, survey=True, ori=s["ori"])
+    assert h_o.sum() > 0
+    assert np.array_equal(h, h_o) and st["overflow"] == ov_o
+
+
+def test_rppi_survey_full_reference_anchors(ref, engine_lib, survey_full):
+    """Survey-mode rppi DDD on the full data catalogue, the reference's own
+    rppi kernel on 64 random anchors: bit for bit."""
+    s = survey_full
+    c1, c2, c3 = _survey_args(s, "DDD", True)
+    sub = random_anchors(c1, 64, 97)
+    edges = api.logspace(1.0, 30.0, 13)
+    t0 = time.perf_counter()
+    h_ref, ov_ref, _, _ = ref.reference_count_rppi(s["box"], edges, 30, sub, c2, c3, survey=True, ori=s["ori"])
+    print(f"\nrppi survey DDD reference: {len(sub)} anchors, {time.perf_counter() - t0:.1f} s")
+    h, st = _rppi_run(s["box"], edges, 30, sub, c2, c3, survey=True, ori=s["ori"])
+    assert h_ref.sum() > 0
+    assert np.array_equal(h, h_ref) and st["overflow"] == ov_ref
